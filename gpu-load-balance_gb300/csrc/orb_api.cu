@@ -1,0 +1,595 @@
+// Host driver and C ABI of the ORB engine (include/orb/orb.h).
+//
+// orb_build runs the reference's master() level loop (src/orbit.cpp:102-275) with every
+// step on the device: per level a plan, histogram/resolve passes that replay the
+// bisection, the parallel Hoare partition and the split. The host only launches and, per
+// bisection pass, reads one flag that says whether any cell of the level is still active.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "orb_internal.cuh"
+
+using namespace orb;
+
+namespace {
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n, bool zero = false) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = n < 16 ? 16 : n;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        cap = want;
+        if (zero) e = cudaMemset(p, 0, want * sizeof(T));
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+int log2_exact(uint32_t d) {
+    int k = 0;
+    while ((1u << k) < d) ++k;
+    return k;
+}
+
+}  // namespace
+
+struct orb_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string err;
+
+    DevBuf<float> x, y, z;
+    DevBuf<uint32_t> idx, tl, tr;
+    DevBuf<orb_cell_t> heap;
+    DevBuf<uint2> ranges;
+    DevBuf<uint32_t> tile_off, hist_off, below, part_s, part_ge, part_le, out_counts;
+    DevBuf<uint8_t> hist_k, state, iters;
+    DevBuf<uint32_t> hist;
+    DevBuf<uint32_t> tile_ge, tile_le, tile_ge_cnt, tile_le_cnt;
+    DevBuf<int> slots;
+    DevBuf<BuildCounters> counters;
+    DevBuf<orb_cell_t> staging;
+    BuildCounters *h_counters = nullptr;  // pinned
+
+    // service layer state
+    bool loaded = false;
+    uint64_t loaded_n = 0;
+    uint32_t loaded_cells = 0;
+};
+
+namespace {
+
+orb_status fail(orb_ctx *ctx, orb_status s, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return s;
+}
+
+orb_status cuda_fail(orb_ctx *ctx, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(ctx, e == cudaErrorMemoryAllocation ? ORB_ERR_OUT_OF_MEMORY : ORB_ERR_CUDA, m);
+}
+
+#define ORB_CUDA(call)                                                   \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);         \
+    } while (0)
+
+bool is_device_ptr(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Level buffers for up to `max_cells` cells per level and `max_tiles` tiles.
+orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, uint32_t heap_cells) {
+    const uint64_t max_tiles = n / kTile + max_cells + 2;
+    const uint64_t max_bins = n / 2 + 16ull * max_cells + 16;
+    ORB_CUDA(ctx->tl.ensure(n + 1));
+    ORB_CUDA(ctx->tr.ensure(n + 1));
+    ORB_CUDA(ctx->heap.ensure(heap_cells));
+    ORB_CUDA(ctx->ranges.ensure(heap_cells));
+    ORB_CUDA(ctx->tile_off.ensure(max_cells + 1));
+    ORB_CUDA(ctx->hist_off.ensure(max_cells + 1));
+    ORB_CUDA(ctx->below.ensure(max_cells));
+    ORB_CUDA(ctx->part_s.ensure(max_cells));
+    ORB_CUDA(ctx->part_ge.ensure(max_cells));
+    ORB_CUDA(ctx->part_le.ensure(max_cells));
+    ORB_CUDA(ctx->out_counts.ensure(max_cells));
+    ORB_CUDA(ctx->hist_k.ensure(max_cells));
+    ORB_CUDA(ctx->state.ensure(max_cells));
+    ORB_CUDA(ctx->iters.ensure(max_cells));
+    ORB_CUDA(ctx->slots.ensure(max_cells));
+    ORB_CUDA(ctx->hist.ensure(max_bins, true));
+    ORB_CUDA(ctx->tile_ge.ensure(max_tiles));
+    ORB_CUDA(ctx->tile_le.ensure(max_tiles));
+    ORB_CUDA(ctx->tile_ge_cnt.ensure(max_tiles));
+    ORB_CUDA(ctx->tile_le_cnt.ensure(max_tiles));
+    ORB_CUDA(ctx->counters.ensure(1, true));
+    return ORB_OK;
+}
+
+Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
+    Level v;
+    std::memset(&v, 0, sizeof v);
+    v.x = x;
+    v.y = y;
+    v.z = z;
+    v.idx = ctx->idx.p;
+    v.heap = ctx->heap.p;
+    v.ranges = ctx->ranges.p;
+    v.slots = nullptr;
+    v.tile_off = ctx->tile_off.p;
+    v.hist_off = ctx->hist_off.p;
+    v.hist_k = ctx->hist_k.p;
+    v.state = ctx->state.p;
+    v.iters = ctx->iters.p;
+    v.hist = ctx->hist.p;
+    v.below = ctx->below.p;
+    v.tile_ge = ctx->tile_ge.p;
+    v.tile_le = ctx->tile_le.p;
+    v.tile_ge_cnt = ctx->tile_ge_cnt.p;
+    v.tile_le_cnt = ctx->tile_le_cnt.p;
+    v.part_s = ctx->part_s.p;
+    v.part_ge = ctx->part_ge.p;
+    v.part_le = ctx->part_le.p;
+    v.tl = ctx->tl.p;
+    v.tr = ctx->tr.p;
+    v.out_counts = ctx->out_counts.p;
+    v.counters = ctx->counters.p;
+    return v;
+}
+
+int pass_grid(orb_ctx *ctx) { return ctx->num_sms * 8; }
+
+// Bisection of every cell of the level to completion (found or capped).
+orb_status run_bisection(orb_ctx *ctx, const Level &v, uint32_t *passes) {
+    for (int pass = 0;; ++pass) {
+        if (pass > 64) return fail(ctx, ORB_ERR_TIMEOUT, "bisection did not finish in 64 passes");
+        ORB_CUDA(cudaMemsetAsync(&ctx->counters.p->any_active, 0, sizeof(uint32_t), ctx->stream));
+        launch_hist(v, pass_grid(ctx), ctx->stream);
+        launch_resolve(v, ctx->stream);
+        ORB_CUDA(cudaGetLastError());
+        ORB_CUDA(cudaMemcpyAsync(&ctx->h_counters->any_active, &ctx->counters.p->any_active,
+                                 sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+        ++*passes;
+        if (!ctx->h_counters->any_active) break;
+    }
+    return ORB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orb_abi_version(void) { return ORB_ABI_VERSION; }
+
+const char *orb_status_string(orb_status s) {
+    switch (s) {
+        case ORB_OK: return "ok";
+        case ORB_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ORB_ERR_CUDA: return "CUDA error";
+        case ORB_ERR_OUT_OF_MEMORY: return "out of memory";
+        case ORB_ERR_CAPACITY: return "capacity exceeded";
+        case ORB_ERR_NOT_LOADED: return "no particles loaded";
+        case ORB_ERR_TIMEOUT: return "timeout";
+    }
+    return "unknown status";
+}
+
+const char *orb_last_error(const orb_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
+    if (!out) return ORB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (opts && opts->flags != 0) return ORB_ERR_INVALID_ARGUMENT;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return ORB_ERR_CUDA;
+    if (device < 0 || device >= count) return ORB_ERR_INVALID_ARGUMENT;
+    orb_ctx *ctx = new (std::nothrow) orb_ctx();
+    if (!ctx) return ORB_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    orb_status st = ORB_OK;
+    do {
+        if ((e = cudaSetDevice(device)) != cudaSuccess) { st = cuda_fail(ctx, e, "cudaSetDevice"); break; }
+        if ((e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaDeviceGetAttribute");
+            break;
+        }
+        if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaStreamCreate");
+            break;
+        }
+        for (auto &ev : ctx->ev)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) { st = cuda_fail(ctx, e, "cudaEventCreate"); break; }
+        if (st != ORB_OK) break;
+        if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaMallocHost");
+            break;
+        }
+        if (opts && (opts->reserve_particles || opts->reserve_leaves)) {
+            uint64_t n = opts->reserve_particles;
+            uint32_t d = opts->reserve_leaves ? opts->reserve_leaves : 1;
+            if (ctx->x.ensure(n) || ctx->y.ensure(n) || ctx->z.ensure(n) || ctx->idx.ensure(n)) {
+                st = fail(ctx, ORB_ERR_OUT_OF_MEMORY, "reserve failed");
+                break;
+            }
+            st = ensure_level_buffers(ctx, n, d, 2 * d - 1);
+        }
+    } while (0);
+    if (st != ORB_OK) {
+        orb_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return ORB_OK;
+}
+
+orb_status orb_ctx_destroy(orb_ctx *ctx) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->x.release(); ctx->y.release(); ctx->z.release();
+    ctx->idx.release(); ctx->tl.release(); ctx->tr.release();
+    ctx->heap.release(); ctx->ranges.release();
+    ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release();
+    ctx->part_s.release(); ctx->part_ge.release(); ctx->part_le.release(); ctx->out_counts.release();
+    ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
+    ctx->tile_ge.release(); ctx->tile_le.release(); ctx->tile_ge_cnt.release(); ctx->tile_le_cnt.release();
+    ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ORB_OK;
+}
+
+orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                     uint32_t levels, const float lower[3], const float upper[3],
+                     orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                     orb_build_info *info) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
+    if ((n > 0 && (!x || !y || !z)) || !heap || !ranges || !lower || !upper)
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
+    if (d == 0 || (d & (d - 1)) != 0)
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "d must be a power of two");
+    if (n >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "n must be below 2^31");
+    if (d > (1u << 30)) return fail(ctx, ORB_ERR_CAPACITY, "d too large");
+    const int ylev = log2_exact(d);
+    if (levels == 0) levels = (uint32_t)ylev;
+    if ((int)levels > ylev) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "levels exceeds log2(d)");
+    const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
+    if (dev && n > 0 && (!is_device_ptr(x) || !is_device_ptr(y) || !is_device_ptr(z) ||
+                         (perm && !is_device_ptr(perm))))
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "ORB_DEVICE_POINTERS set but a pointer is not device memory");
+
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t heap_cells = 2 * d - 1;
+    const uint32_t max_cells = levels ? (1u << (levels - 1)) : 1u;
+    orb_status st = ensure_level_buffers(ctx, n, max_cells, heap_cells);
+    if (st != ORB_OK) return st;
+    ORB_CUDA(ctx->idx.ensure(n + 1));
+    float *dx = x, *dy = y, *dz = z;
+    cudaStream_t s = ctx->stream;
+    float h2d_ms = 0.f, d2h_ms = 0.f;
+    if (!dev) {
+        ORB_CUDA(ctx->x.ensure(n + 1));
+        ORB_CUDA(ctx->y.ensure(n + 1));
+        ORB_CUDA(ctx->z.ensure(n + 1));
+        dx = ctx->x.p;
+        dy = ctx->y.p;
+        dz = ctx->z.p;
+        ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
+        if (n) {
+            ORB_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(float), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, s));
+        }
+        ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+    }
+    ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
+    Level v = make_level(ctx, dx, dy, dz);
+    launch_init(v, n, lower, upper, d, (int)heap_cells, s);
+    ORB_CUDA(cudaGetLastError());
+    uint32_t passes = 0;
+    for (uint32_t l = 1; l <= levels; ++l) {
+        v.base = (1 << (l - 1)) - 1;  // src/orbit.cpp:104-107
+        v.C = 1 << (l - 1);
+        launch_plan(v, s);
+        st = run_bisection(ctx, v, &passes);
+        if (st != ORB_OK) return st;
+        launch_partition(v, pass_grid(ctx), true, s);
+        ORB_CUDA(cudaGetLastError());
+    }
+    ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    if (!dev) {
+        ORB_CUDA(cudaStreamSynchronize(s));
+        ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
+        ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
+        if (n) {
+            ORB_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+            ORB_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+            ORB_CUDA(cudaMemcpyAsync(z, dz, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+        }
+    }
+    if (perm && n)
+        ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n * sizeof(uint32_t),
+                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    ORB_CUDA(cudaMemcpyAsync(heap, ctx->heap.p, heap_cells * sizeof(orb_cell_t), cudaMemcpyDeviceToHost, s));
+    ORB_CUDA(cudaMemcpyAsync(ranges, ctx->ranges.p, heap_cells * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    ORB_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, sizeof(BuildCounters), cudaMemcpyDeviceToHost, s));
+    if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+    ORB_CUDA(cudaStreamSynchronize(s));
+    float dev_ms = 0.f;
+    ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
+    if (!dev) ORB_CUDA(cudaEventElapsedTime(&d2h_ms, ctx->ev[2], ctx->ev[3]));
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->levels_built = levels;
+        info->degenerate_cells = ctx->h_counters->degenerate;
+        info->zero_volume_cells = ctx->h_counters->zero_volume;
+        info->unfound_cells = ctx->h_counters->unfound;
+        info->max_iterations = ctx->h_counters->max_iters;
+        info->count_passes = passes;
+        info->device_ms = dev_ms;
+        info->h2d_ms = h2d_ms;
+        info->d2h_ms = d2h_ms;
+    }
+    return ORB_OK;
+}
+
+orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float *x, float *y,
+                        float *z, uint32_t flags) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (kind != ORB_GEN_UNIFORM && kind != ORB_GEN_PLUMMER)
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown generator kind");
+    if (n == 0) return ORB_OK;
+    if (!x || !y || !z) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
+    float *dx = x, *dy = y, *dz = z;
+    if (!dev) {
+        ORB_CUDA(ctx->x.ensure(n));
+        ORB_CUDA(ctx->y.ensure(n));
+        ORB_CUDA(ctx->z.ensure(n));
+        dx = ctx->x.p;
+        dy = ctx->y.p;
+        dz = ctx->z.p;
+    }
+    if (kind == ORB_GEN_UNIFORM) {
+        launch_gen_uniform(seed, n, dx, dy, dz, ctx->stream);
+    } else {
+        // Cluster table, computed on the host exactly as the CPU oracle computes it.
+        float centres[64 * 3];
+        double scales[64];
+        auto mix64 = [](uint64_t zz) {
+            zz += 0x9E3779B97F4A7C15ull;
+            zz = (zz ^ (zz >> 30)) * 0xBF58476D1CE4E5B9ull;
+            zz = (zz ^ (zz >> 27)) * 0x94D049BB133111EBull;
+            return zz ^ (zz >> 31);
+        };
+        auto draw = [&](uint64_t sd, uint64_t c) { return mix64(mix64(sd) + c * 0xD1B54A32D192ED03ull); };
+        const uint64_t dom = seed ^ 0xC1A57E5C1A57E5C1ull;
+        for (int k = 0; k < 64; ++k) {
+            for (int a = 0; a < 3; ++a) {
+                volatile float f = (float)(uint32_t)(draw(dom, 4 * k + a) >> 40);
+                volatile float g = f * 0x1p-24f;
+                centres[3 * k + a] = g - 0.5f;
+            }
+            double u = (double)(draw(dom, 4 * k + 3) >> 11) * 0x1p-53;
+            scales[k] = 0.005 * std::pow(10.0, u);
+        }
+        launch_gen_plummer(seed, n, centres, scales, dx, dy, dz, ctx->stream);
+    }
+    ORB_CUDA(cudaGetLastError());
+    if (!dev) {
+        ORB_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        ORB_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        ORB_CUDA(cudaMemcpyAsync(z, dz, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ORB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Service layer
+// ---------------------------------------------------------------------------------------
+orb_status orb_load_particles(orb_ctx *ctx, const float *x, const float *y, const float *z,
+                              uint64_t n, uint32_t max_cells, uint32_t flags) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if ((n > 0 && (!x || !y || !z)) || max_cells == 0)
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer or max_cells == 0");
+    if (n >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "n must be below 2^31");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    orb_status st = ensure_level_buffers(ctx, n, max_cells, max_cells);
+    if (st != ORB_OK) return st;
+    ORB_CUDA(ctx->x.ensure(n + 1));
+    ORB_CUDA(ctx->y.ensure(n + 1));
+    ORB_CUDA(ctx->z.ensure(n + 1));
+    ORB_CUDA(ctx->idx.ensure(n + 1));
+    ORB_CUDA(ctx->staging.ensure(max_cells));
+    const cudaMemcpyKind k = (flags & ORB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (n) {
+        ORB_CUDA(cudaMemcpyAsync(ctx->x.p, x, n * sizeof(float), k, s));
+        ORB_CUDA(cudaMemcpyAsync(ctx->y.p, y, n * sizeof(float), k, s));
+        ORB_CUDA(cudaMemcpyAsync(ctx->z.p, z, n * sizeof(float), k, s));
+    }
+    // identity permutation and range map {root = [0, n)} (src/services/init.cu:63-66)
+    std::vector<uint32_t> iota(n);
+    for (uint64_t i = 0; i < n; ++i) iota[i] = (uint32_t)i;
+    if (n) ORB_CUDA(cudaMemcpyAsync(ctx->idx.p, iota.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    ORB_CUDA(cudaMemsetAsync(ctx->ranges.p, 0, max_cells * sizeof(uint2), s));
+    uint2 root = make_uint2(0u, (uint32_t)n);
+    ORB_CUDA(cudaMemcpyAsync(ctx->ranges.p, &root, sizeof root, cudaMemcpyHostToDevice, s));
+    ORB_CUDA(cudaMemsetAsync(ctx->counters.p, 0, sizeof(BuildCounters), s));
+    ORB_CUDA(cudaStreamSynchronize(s));
+    ctx->loaded = true;
+    ctx->loaded_n = n;
+    ctx->loaded_cells = max_cells;
+    return ORB_OK;
+}
+
+orb_status orb_store_particles(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *perm,
+                               uint32_t flags) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!ctx->loaded) return fail(ctx, ORB_ERR_NOT_LOADED, "no particles loaded");
+    const uint64_t n = ctx->loaded_n;
+    if (n && (!x || !y || !z)) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    const cudaMemcpyKind k = (flags & ORB_DEVICE_POINTERS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaStream_t s = ctx->stream;
+    if (n) {
+        ORB_CUDA(cudaMemcpyAsync(x, ctx->x.p, n * sizeof(float), k, s));
+        ORB_CUDA(cudaMemcpyAsync(y, ctx->y.p, n * sizeof(float), k, s));
+        ORB_CUDA(cudaMemcpyAsync(z, ctx->z.p, n * sizeof(float), k, s));
+        if (perm) ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n * sizeof(uint32_t), k, s));
+    }
+    ORB_CUDA(cudaStreamSynchronize(s));
+    return ORB_OK;
+}
+
+static orb_status service_prepare(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells,
+                                  bool need_children, Level *out) {
+    if (!ctx->loaded) return fail(ctx, ORB_ERR_NOT_LOADED, "no particles loaded");
+    if (n_cells && !cells) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null cells");
+    std::vector<uint8_t> seen(ctx->loaded_cells, 0);
+    std::vector<int> ids(n_cells);
+    for (uint32_t i = 0; i < n_cells; ++i) {
+        const int64_t id = cells[i].id;
+        const int64_t hi = need_children ? 2 * id + 2 : id;
+        if (id < 0 || hi >= (int64_t)ctx->loaded_cells)
+            return fail(ctx, ORB_ERR_CAPACITY, "cell id outside the range map");
+        if (seen[id]) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "duplicate cell id");
+        seen[id] = 1;
+        ids[i] = (int)id;
+    }
+    cudaStream_t s = ctx->stream;
+    // Each cell is placed at heap slot == id, so child slots are 2id+1 and 2id+2.
+    if (n_cells) {
+        ORB_CUDA(cudaMemcpyAsync(ctx->slots.p, ids.data(), n_cells * sizeof(int), cudaMemcpyHostToDevice, s));
+        for (uint32_t i = 0; i < n_cells; ++i)
+            ORB_CUDA(cudaMemcpyAsync(ctx->heap.p + ids[i], cells + i, sizeof(orb_cell_t), cudaMemcpyHostToDevice, s));
+    }
+    Level v = make_level(ctx, ctx->x.p, ctx->y.p, ctx->z.p);
+    v.slots = ctx->slots.p;
+    v.base = 0;
+    v.C = (int)n_cells;
+    *out = v;
+    return ORB_OK;
+}
+
+orb_status orb_count(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells, uint32_t *out) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!ctx->loaded) return fail(ctx, ORB_ERR_NOT_LOADED, "no particles loaded");
+    if (n_cells && (!cells || !out)) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    std::vector<uint2> rg(ctx->loaded_cells);
+    ORB_CUDA(cudaMemcpyAsync(rg.data(), ctx->ranges.p, rg.size() * sizeof(uint2), cudaMemcpyDeviceToHost, ctx->stream));
+    ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t i = 0; i < n_cells; ++i) {
+        const int64_t id = cells[i].id;
+        if (id < 0 || id >= (int64_t)ctx->loaded_cells)
+            return fail(ctx, ORB_ERR_CAPACITY, "cell id outside the range map");
+        out[i] = rg[id].y - rg[id].x;  // src/services/count.cpp:14-17
+    }
+    return ORB_OK;
+}
+
+orb_status orb_count_left(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells, uint32_t *out) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (n_cells && !out) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null out");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    Level v;
+    orb_status st = service_prepare(ctx, cells, n_cells, false, &v);
+    if (st != ORB_OK || n_cells == 0) return st;
+    cudaStream_t s = ctx->stream;
+    ORB_CUDA(cudaMemsetAsync(ctx->out_counts.p, 0, n_cells * sizeof(uint32_t), s));
+    launch_plan(v, s);
+    launch_count_left(v, pass_grid(ctx), s);
+    ORB_CUDA(cudaGetLastError());
+    std::vector<uint32_t> res(n_cells);
+    ORB_CUDA(cudaMemcpyAsync(res.data(), ctx->out_counts.p, n_cells * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    ORB_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < n_cells; ++i)
+        if (!cells[i].foundCut) out[i] = res[i];  // src/services/countLeft.cpp:19-21
+    return ORB_OK;
+}
+
+orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    Level v;
+    orb_status st = service_prepare(ctx, cells, n_cells, true, &v);
+    if (st != ORB_OK || n_cells == 0) return st;
+    cudaStream_t s = ctx->stream;
+    launch_plan(v, s);
+    launch_partition(v, pass_grid(ctx), false, s);
+    ORB_CUDA(cudaGetLastError());
+    ORB_CUDA(cudaStreamSynchronize(s));
+    return ORB_OK;
+}
+
+orb_status orb_get_ranges(orb_ctx *ctx, uint32_t *ranges, uint32_t n_cells) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!ctx->loaded) return fail(ctx, ORB_ERR_NOT_LOADED, "no particles loaded");
+    if (!ranges || n_cells > ctx->loaded_cells) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "bad range request");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    ORB_CUDA(cudaMemcpyAsync(ranges, ctx->ranges.p, n_cells * sizeof(uint2), cudaMemcpyDeviceToHost, ctx->stream));
+    ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ORB_OK;
+}
+
+orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!ctx->loaded) return fail(ctx, ORB_ERR_NOT_LOADED, "no particles loaded");
+    if (!ranges || n_cells > ctx->loaded_cells) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "bad range request");
+    for (uint32_t i = 0; i < n_cells; ++i)
+        if (ranges[2 * i] > ranges[2 * i + 1] || ranges[2 * i + 1] > ctx->loaded_n)
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "range outside the loaded particles");
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    ORB_CUDA(cudaMemcpyAsync(ctx->ranges.p, ranges, n_cells * sizeof(uint2), cudaMemcpyHostToDevice, ctx->stream));
+    ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ORB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,101 @@
+// Internal declarations of the ORB engine: device helpers shared by the kernels and the
+// launch interface the host driver uses. Nothing here is part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "orb/orb.h"
+
+namespace orb {
+
+static_assert(sizeof(orb_cell_t) == 52, "orb_cell_t must keep the reference's 52-byte Cell layout");
+
+constexpr int kMaxIterations = 32;   // bisection cap, src/orbit.cpp:149
+constexpr int kTile = 8192;          // keys per tile of the multi-CTA passes
+constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
+constexpr int kThreads = 256;
+
+enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2 };
+
+// Device-side counters of one build (read back at the end).
+struct BuildCounters {
+    uint32_t degenerate;
+    uint32_t zero_volume;
+    uint32_t unfound;
+    uint32_t max_iters;
+    uint32_t any_active;  // set by the resolve step when a cell still needs a pass
+    uint32_t pad[3];
+};
+
+// Everything a level's kernels need. Cells of the level are heap slots [base, base + C)
+// unless `slots` is non-null (service calls over an arbitrary cell list).
+struct Level {
+    float *x, *y, *z;
+    uint32_t *idx;          // original particle index (perm), may be null
+    orb_cell_t *heap;
+    uint2 *ranges;          // {begin, end} per heap slot, absolute positions
+    const int *slots;       // optional explicit slot list [C]
+    int base;
+    int C;
+    // plan
+    uint32_t *tile_off;     // [C+1] first tile of each cell
+    uint32_t *hist_off;     // [C+1] first bin of each cell in the histogram pool
+    uint8_t *hist_k;        // [C]   tree depth of each cell's histogram
+    uint8_t *state;         // [C]   CellState
+    uint8_t *iters;         // [C]   bisection iterations done
+    uint32_t *hist;         // histogram pool (kept all-zero between passes)
+    uint32_t *below;        // [C]   keys below the left margin in the current pass
+    // partition
+    uint32_t *tile_ge;      // [tiles] keys >= cut per tile, then exclusive prefix in-cell
+    uint32_t *tile_le;      // [tiles] keys <= cut per tile, then exclusive prefix in-cell
+    uint32_t *tile_ge_cnt;  // [tiles] raw counts kept for the table pass
+    uint32_t *tile_le_cnt;
+    uint32_t *part_s;       // [C] number of Hoare swaps
+    uint32_t *part_ge;      // [C] keys >= cut in the cell
+    uint32_t *part_le;      // [C] keys <= cut in the cell
+    uint32_t *tl;           // [N] positions of keys >= cut from the left (by rank)
+    uint32_t *tr;           // [N] positions of keys <= cut from the right (by rank)
+    uint32_t *out_counts;   // service calls: per-cell result
+    BuildCounters *counters;
+};
+
+__device__ __forceinline__ int level_slot(const Level &v, int c) {
+    return v.slots ? v.slots[c] : v.base + c;
+}
+
+__device__ __forceinline__ int eff_axis(int a) { return a < 0 ? 0 : a; }
+
+// getCut(), src/cell.h:74-76: float sum, halved (exact, no FMA, no FTZ).
+__device__ __forceinline__ float mid_cut(float lo, float hi) {
+    return __fmul_rn(__fadd_rn(hi, lo), 0.5f);
+}
+
+// src/orbit.cpp:204-208 for an even nLeafCells (ratio = 0.5f exactly; d is a power of two,
+// so every bisected cell has an even leaf count). Returns 0 found, +1 right margin, -1 left.
+__device__ __forceinline__ int convergence(uint32_t count_left, uint32_t count) {
+    float prod = __fmul_rn(__uint2float_rn(count), 0.5f);
+    float diff = __fsub_rn(__uint2float_rn(count_left), prod);
+    int difference = __float2int_rz(diff);
+    if (difference > -3 && difference < 3) return 0;
+    return difference > 0 ? 1 : -1;
+}
+
+__device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {
+    return axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
+}
+
+// Host-side launchers (orb_kernels.cu).
+void launch_init(const Level &v, uint64_t n, const float lower[3], const float upper[3],
+                 uint32_t d, int heap_cells, cudaStream_t st);
+void launch_plan(const Level &v, cudaStream_t st);
+void launch_hist(const Level &v, int grid, cudaStream_t st);
+void launch_resolve(const Level &v, cudaStream_t st);
+void launch_partition(const Level &v, int grid, bool do_split, cudaStream_t st);
+void launch_count_left(const Level &v, int grid, cudaStream_t st);
+void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
+                        cudaStream_t st);
+void launch_gen_plummer(uint64_t seed, uint64_t n, const float *centres, const double *scales,
+                        float *x, float *y, float *z, cudaStream_t st);
+
+}  // namespace orb

@@ -1,0 +1,296 @@
+"""Python front end of the GB300 ORB engine: builds liborb_gb300.so and binds its C ABI.
+
+The engine itself is C++/CUDA behind the C ABI declared in include/orb/orb.h; this module
+only compiles it (nvcc, sm_103a) and calls it through ctypes. There is no Python or CPU
+compute path: every call fails with OrbError if the library cannot be loaded.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "liborb_gb300.so")
+SOURCES = ["orb_kernels.cu", "orb_api.cu"]
+HEADERS = ["orb_internal.cuh"]
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+
+CELL_DTYPE = np.dtype(
+    [
+        ("id", "<i4"),
+        ("nLeafCells", "<i4"),
+        ("prevCutAxis", "<i4"),
+        ("cutAxis", "<i4"),
+        ("foundCut", "u1"),
+        ("pad_", "u1", (3,)),
+        ("cutMarginLeft", "<f4"),
+        ("cutMarginRight", "<f4"),
+        ("lower", "<f4", (3,)),
+        ("upper", "<f4", (3,)),
+    ]
+)
+assert CELL_DTYPE.itemsize == 52
+
+ORB_DEVICE_POINTERS = 0x1
+ORB_GEN_UNIFORM = 0
+ORB_GEN_PLUMMER = 1
+
+STATUS = {
+    0: "ok",
+    1: "invalid argument",
+    2: "CUDA error",
+    3: "out of memory",
+    4: "capacity exceeded",
+    5: "no particles loaded",
+    6: "timeout",
+}
+
+# Every symbol include/orb/orb.h declares (checked by the CPU tests).
+EXPORTS = [
+    "orb_abi_version", "orb_status_string", "orb_last_error", "orb_ctx_create",
+    "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
+    "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
+]
+
+
+class OrbError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}" if msg else STATUS.get(status, str(status)))
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(INCLUDE, "orb", "orb.h")]
+    return any(os.path.getmtime(p) > t for p in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the CUDA sources for sm_103a (in parallel) and link liborb_gb300.so."""
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    objs = []
+
+    def compile_one(src):
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class BuildInfo(ctypes.Structure):
+    _fields_ = [
+        ("levels_built", ctypes.c_uint32),
+        ("degenerate_cells", ctypes.c_uint32),
+        ("zero_volume_cells", ctypes.c_uint32),
+        ("unfound_cells", ctypes.c_uint32),
+        ("max_iterations", ctypes.c_uint32),
+        ("count_passes", ctypes.c_uint32),
+        ("device_ms", ctypes.c_float),
+        ("h2d_ms", ctypes.c_float),
+        ("d2h_ms", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("reserve_particles", ctypes.c_uint64), ("reserve_leaves", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the engine library (it must already be built; see build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OrbError(2, f"engine library not built: {path} (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    u32 = ctypes.c_uint32
+    u64 = ctypes.c_uint64
+    L.orb_abi_version.restype = ctypes.c_int
+    L.orb_status_string.restype = ctypes.c_char_p
+    L.orb_status_string.argtypes = [ctypes.c_int]
+    L.orb_last_error.restype = ctypes.c_char_p
+    L.orb_last_error.argtypes = [vp]
+    L.orb_ctx_create.restype = ctypes.c_int
+    L.orb_ctx_create.argtypes = [ctypes.c_int, ctypes.POINTER(Opts), ctypes.POINTER(vp)]
+    L.orb_ctx_destroy.restype = ctypes.c_int
+    L.orb_ctx_destroy.argtypes = [vp]
+    L.orb_build.restype = ctypes.c_int
+    L.orb_build.argtypes = [vp, vp, vp, vp, u64, u32, u32, vp, vp, vp, vp, vp, u32,
+                            ctypes.POINTER(BuildInfo)]
+    L.orb_load_particles.restype = ctypes.c_int
+    L.orb_load_particles.argtypes = [vp, vp, vp, vp, u64, u32, u32]
+    L.orb_store_particles.restype = ctypes.c_int
+    L.orb_store_particles.argtypes = [vp, vp, vp, vp, vp, u32]
+    for name in ("orb_count", "orb_count_left"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = [vp, vp, u32, vp]
+    L.orb_partition.restype = ctypes.c_int
+    L.orb_partition.argtypes = [vp, vp, u32]
+    for name in ("orb_get_ranges", "orb_set_ranges"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = [vp, vp, u32]
+    L.orb_generate.restype = ctypes.c_int
+    L.orb_generate.argtypes = [vp, ctypes.c_int, u64, u64, vp, vp, vp, u32]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):  # torch tensor
+        return a.data_ptr()
+    return int(a)
+
+
+@dataclass
+class BuildResult:
+    heap: np.ndarray      # CELL_DTYPE[2d-1]
+    ranges: np.ndarray    # uint32[2d-1, 2]
+    perm: object          # uint32[n] (numpy) or the device tensor passed in
+    info: dict
+
+
+class Context:
+    """One engine context on one CUDA device (owns a stream and device buffers)."""
+
+    def __init__(self, device: int = 0, reserve_particles: int = 0, reserve_leaves: int = 0):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        o = Opts(reserve_particles, reserve_leaves, 0)
+        self._check(self.lib.orb_ctx_create(device, ctypes.byref(o), ctypes.byref(self.h)))
+
+    def _check(self, st):
+        if st != 0:
+            msg = self.lib.orb_last_error(self.h).decode() if self.h else ""
+            raise OrbError(st, msg)
+
+    def close(self):
+        if self.h:
+            self.lib.orb_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, x, y, z, d: int, levels: int = 0, lower=(-0.5, -0.5, -0.5),
+              upper=(0.5, 0.5, 0.5), perm=True, device_pointers: bool = False) -> BuildResult:
+        """ORB build. Host numpy arrays are partitioned in place; with device_pointers the
+        arguments are device tensors/pointers partitioned in place on the device."""
+        n = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        heap = np.zeros(2 * d - 1, CELL_DTYPE)
+        ranges = np.zeros((2 * d - 1, 2), np.uint32)
+        if perm is True:
+            perm = np.empty(n, np.uint32)
+        lo = np.asarray(lower, np.float32)
+        hi = np.asarray(upper, np.float32)
+        info = BuildInfo()
+        st = self.lib.orb_build(self.h, _ptr(x), _ptr(y), _ptr(z), n, d, levels, lo.ctypes.data,
+                                hi.ctypes.data, heap.ctypes.data, ranges.ctypes.data, _ptr(perm),
+                                ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
+        self._check(st)
+        return BuildResult(heap, ranges, perm, info.as_dict())
+
+    def generate(self, kind: int, seed: int, n: int, x, y, z, device_pointers: bool = False):
+        self._check(self.lib.orb_generate(self.h, kind, seed, n, _ptr(x), _ptr(y), _ptr(z),
+                                          ORB_DEVICE_POINTERS if device_pointers else 0))
+
+    def generate_host(self, kind: int, seed: int, n: int):
+        x, y, z = (np.empty(n, np.float32) for _ in range(3))
+        self.generate(kind, seed, n, x, y, z)
+        return x, y, z
+
+    # service layer -------------------------------------------------------------------
+    def load_particles(self, x, y, z, max_cells: int, device_pointers: bool = False):
+        n = int(x.shape[0])
+        self._check(self.lib.orb_load_particles(self.h, _ptr(x), _ptr(y), _ptr(z), n, max_cells,
+                                                ORB_DEVICE_POINTERS if device_pointers else 0))
+        self.loaded_n = n
+
+    def store_particles(self):
+        n = self.loaded_n
+        x, y, z = (np.empty(n, np.float32) for _ in range(3))
+        perm = np.empty(n, np.uint32)
+        self._check(self.lib.orb_store_particles(self.h, x.ctypes.data, y.ctypes.data,
+                                                 z.ctypes.data, perm.ctypes.data, 0))
+        return x, y, z, perm
+
+    def count(self, cells: np.ndarray) -> np.ndarray:
+        out = np.zeros(len(cells), np.uint32)
+        self._check(self.lib.orb_count(self.h, cells.ctypes.data, len(cells), out.ctypes.data))
+        return out
+
+    def count_left(self, cells: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.zeros(len(cells), np.uint32) if out is None else out
+        self._check(self.lib.orb_count_left(self.h, cells.ctypes.data, len(cells), out.ctypes.data))
+        return out
+
+    def partition(self, cells: np.ndarray):
+        self._check(self.lib.orb_partition(self.h, cells.ctypes.data, len(cells)))
+
+    def get_ranges(self, n_cells: int) -> np.ndarray:
+        r = np.zeros((n_cells, 2), np.uint32)
+        self._check(self.lib.orb_get_ranges(self.h, r.ctypes.data, n_cells))
+        return r
+
+    def set_ranges(self, ranges: np.ndarray):
+        r = np.ascontiguousarray(ranges, np.uint32)
+        self._check(self.lib.orb_set_ranges(self.h, r.ctypes.data, r.shape[0]))

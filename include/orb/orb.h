@@ -1,0 +1,159 @@
+/*
+ * orb.h: C ABI of the GB300 ORB (orthogonal recursive bisection) engine.
+ *
+ * The engine builds the reference's ORB cell tree on one GPU (sm_103a): float32 particles
+ * go in; the particles come back reordered so that every cell's particles are contiguous,
+ * together with the cell heap (the reference's 52-byte struct Cell) and the cell-to-range
+ * map. Results are bit-exact with the reference's CPU path (orbit mode o=0).
+ *
+ * Every call returns an orb_status and never exits the process. A context owns one CUDA
+ * stream and its device buffers; calls on one context must not run concurrently from
+ * several host threads (use one context per thread).
+ *
+ * Reference interfaces replaced (paths within andrinr/gpu-load-balance):
+ *   orb_build          the master() driver of src/orbit.cpp:22-289 (particles in, heap out)
+ *   orb_load_particles ServiceInit + ServiceCopyParticles (src/services/init.cu:27-144,
+ *                      src/services/copyParticles.cu:10-60)
+ *   orb_count          ServiceCount::Service (src/services/count.cpp:8-19)
+ *   orb_count_left     ServiceCountLeft::Service (src/services/countLeft.cpp:9-42), the CPU
+ *                      rule `key < cut` and the skip of cells whose cut is found; it replaces
+ *                      ServiceCountLeftGPUAxis (src/services/countLeftGPUAxis.cu:188-259)
+ *   orb_partition      ServicePartition::Service (src/services/partition.cpp:18-65)
+ *   orb_get_ranges / orb_set_ranges   LocalData::cellToRangeMap (src/services/pst.h:6-41)
+ *   orb_store_particles  the particle array the services leave partitioned in LocalData
+ */
+#ifndef ORB_ORB_H
+#define ORB_ORB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORB_ABI_VERSION 1
+
+typedef enum orb_status {
+    ORB_OK = 0,
+    ORB_ERR_INVALID_ARGUMENT = 1, /* null pointer, d not a power of two, levels > log2(d) ... */
+    ORB_ERR_CUDA = 2,             /* a CUDA runtime call failed; see orb_last_error */
+    ORB_ERR_OUT_OF_MEMORY = 3,    /* a device or pinned allocation failed */
+    ORB_ERR_CAPACITY = 4,         /* the request exceeds a limit of the engine */
+    ORB_ERR_NOT_LOADED = 5,       /* a service call before orb_load_particles */
+    ORB_ERR_TIMEOUT = 6           /* a bounded device wait gave up */
+} orb_status;
+
+/*
+ * Byte-for-byte the reference's struct Cell (src/cell.h:9-17), 52 bytes:
+ * id@0 nLeafCells@4 prevCutAxis@8 cutAxis@12 foundCut@16 cutMarginLeft@20
+ * cutMarginRight@24 lower@28 upper@40. The cut of a cell is
+ * (float)((double)(cutMarginRight + cutMarginLeft) / 2.0) (src/cell.h:74-76).
+ */
+typedef struct orb_cell {
+    int32_t id;
+    int32_t nLeafCells;
+    int32_t prevCutAxis;
+    int32_t cutAxis;
+    uint8_t foundCut;
+    uint8_t pad_[3];
+    float cutMarginLeft;
+    float cutMarginRight;
+    float lower[3];
+    float upper[3];
+} orb_cell_t;
+
+typedef struct orb_ctx orb_ctx;
+
+typedef struct orb_opts {
+    uint64_t reserve_particles; /* pre-size device buffers for this many particles (0 = lazy) */
+    uint32_t reserve_leaves;    /* pre-size cell buffers for this many leaves (0 = lazy) */
+    uint32_t flags;             /* reserved, must be 0 */
+} orb_opts;
+
+/* orb_build / orb_load_particles / orb_store_particles flags */
+#define ORB_DEVICE_POINTERS 0x1u /* x,y,z (and perm) are device pointers; x,y,z are
+                                    partitioned in place on the device */
+
+typedef struct orb_build_info {
+    uint32_t levels_built;
+    uint32_t degenerate_cells;  /* Hoare scan clamped at the cell end: every key below the
+                                   cut, including empty cells (the reference reads and
+                                   swaps outside the cell there, partition.cpp:38,52) */
+    uint32_t zero_volume_cells; /* setCutAxis found no positive extent (cutAxis = -1) */
+    uint32_t unfound_cells;     /* bisection stopped by the 32-sweep cap (orbit.cpp:149) */
+    uint32_t max_iterations;    /* most bisection iterations any cell used */
+    uint32_t count_passes;      /* device passes over cell keys used by the bisection */
+    float device_ms;            /* device time of the build (CUDA events on the ctx stream) */
+    float h2d_ms;               /* host->device copy time (host-pointer calls) */
+    float d2h_ms;               /* device->host copy time (host-pointer calls) */
+} orb_build_info;
+
+/* Context lifetime. device = CUDA ordinal. opts may be NULL. */
+orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out);
+orb_status orb_ctx_destroy(orb_ctx *ctx);
+const char *orb_status_string(orb_status s);
+/* Text of the last error on this context (empty string if none). */
+const char *orb_last_error(const orb_ctx *ctx);
+int orb_abi_version(void);
+
+/*
+ * Build the ORB tree of n particles into d leaf cells (d a power of two).
+ *   x, y, z   n coordinates each, partitioned in place (reference order after the build)
+ *   levels    split levels: 0 selects log2(d) (d leaves); log2(d)-1 is the reference
+ *             driver's own loop bound (src/orbit.cpp:102) and gives d/2 leaves
+ *   lower, upper  root box (the reference uses [-0.5,0.5]^3, src/orbit.cpp:45-46)
+ *   heap      out: 2d-1 cells; cells deeper than `levels` are zeroed
+ *   ranges    out: 2*(2d-1) uint32, {begin,end} per heap cell (cellToRangeMap)
+ *   perm      out, optional (NULL): original index of the particle now at each position
+ *   flags     ORB_DEVICE_POINTERS: x,y,z,perm are device pointers (heap/ranges stay host)
+ *   info      out, optional
+ * n must be below 2^31 (the reference's int indices).
+ */
+orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                     uint32_t levels, const float lower[3], const float upper[3],
+                     orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                     orb_build_info *info);
+
+/*
+ * Service layer: the reference's per-rank services over particles resident in the context.
+ * orb_load_particles copies n particles in (host or device per flags), sets the range map
+ * to root = [0, n) and sizes it for cell ids below max_cells.
+ */
+orb_status orb_load_particles(orb_ctx *ctx, const float *x, const float *y, const float *z,
+                              uint64_t n, uint32_t max_cells, uint32_t flags);
+/* Copies the resident (partitioned) particles out; perm optional. */
+orb_status orb_store_particles(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *perm,
+                               uint32_t flags);
+/* out[i] = end - begin of cells[i] (host arrays). */
+orb_status orb_count(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells, uint32_t *out);
+/* out[i] = #{p in cell i : key[p] < getCut(cell i)} on cutAxis; found cells are skipped
+   (out[i] left untouched), as src/services/countLeft.cpp:19-21. */
+orb_status orb_count_left(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells,
+                          uint32_t *out);
+/* Hoare-partition every cell at getCut() on cutAxis and set the children's ranges
+   (ids 2*id+1, 2*id+2), as src/services/partition.cpp:18-65. */
+orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells);
+/* Range map access: 2*n_cells uint32 for cell ids [0, n_cells). */
+orb_status orb_get_ranges(orb_ctx *ctx, uint32_t *ranges, uint32_t n_cells);
+orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells);
+
+/*
+ * Seeded synthetic particles (the engine's own generator; the reference's xorshf96 input,
+ * src/services/init.cu:11-25, is replaced by a counter-based generator so every size and
+ * seed is reproducible).
+ *   kind ORB_GEN_UNIFORM: i.i.d. on the 2^-24 grid of [-0.5,0.5)^3
+ *   kind ORB_GEN_PLUMMER: 90% from 64 Plummer spheres (scale radii log-uniform in
+ *                         [0.005,0.05)), 10% uniform background, clipped to the box
+ * Writes n floats to each of x,y,z (device pointers if ORB_DEVICE_POINTERS, else host).
+ */
+#define ORB_GEN_UNIFORM 0
+#define ORB_GEN_PLUMMER 1
+orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float *x, float *y,
+                        float *z, uint32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ORB_ORB_H */

@@ -1,0 +1,508 @@
+// ORB oracle: CPU restatement of the reference's o=0 path. TEST INFRASTRUCTURE ONLY.
+// The product library never links or calls this file. Build with -ffp-contract=off so the
+// float32 control arithmetic is evaluated as separately rounded operations, as the
+// reference's x86-64 build does.
+#include "orb_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Seeded counter-based generator (splitmix64 finaliser). Identical in the engine's
+// device generator; tests compare the two bit for bit.
+// ---------------------------------------------------------------------------------------
+inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+inline uint64_t draw(uint64_t seed, uint64_t counter) {
+    return mix64(mix64(seed) + counter * 0xD1B54A32D192ED03ull);
+}
+
+// 24 random bits on the 2^-24 grid of [-0.5, 0.5): exact in float32.
+inline float unit_coord(uint64_t u) {
+    return (float)(uint32_t)(u >> 40) * 0x1p-24f - 0.5f;
+}
+
+inline double unit_double(uint64_t u) { return (double)(u >> 11) * 0x1p-53; }
+
+constexpr uint64_t kClusterDomain = 0xC1A57E5C1A57E5C1ull;
+constexpr int kClusters = 64;
+constexpr uint64_t kPlummerStride = 64;  // counters reserved per particle
+
+template <class F>
+void parallel_chunks(uint64_t n, int nthreads, F &&f) {
+    if (nthreads <= 1 || n < (1u << 16)) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    uint64_t chunk = (n + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; ++t) {
+        uint64_t b = t * chunk, e = std::min<uint64_t>(n, b + chunk);
+        if (b >= e) break;
+        th.emplace_back([&f, b, e] { f(b, e); });
+    }
+    for (auto &t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------------------
+// Reference Cell semantics (src/cell.h).
+// ---------------------------------------------------------------------------------------
+using Cell = oracle_cell_t;
+static_assert(sizeof(Cell) == 52, "Cell must keep the reference's 52-byte layout");
+
+Cell make_cell(int id, int n_leaf, const float *lower, const float *upper) {  // cell.h:19-45
+    Cell c;
+    std::memset(&c, 0, sizeof c);
+    c.id = id;
+    c.nLeafCells = n_leaf;
+    c.foundCut = 0;
+    c.prevCutAxis = -1;
+    c.cutAxis = -1;
+    c.cutMarginLeft = 0.0f;
+    c.cutMarginRight = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        c.lower[k] = lower[k];
+        c.upper[k] = upper[k];
+    }
+    return c;
+}
+
+inline float get_cut(const Cell &c) {  // cell.h:74-76
+    return (float)((double)(c.cutMarginRight + c.cutMarginLeft) / 2.0);
+}
+
+inline int eff_axis(const Cell &c) { return c.cutAxis < 0 ? 0 : c.cutAxis; }
+
+void set_cut_axis(Cell &c, uint32_t *zero_volume) {  // cell.h:102-121
+    int max_d = -1;
+    float max_size = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        float size = c.upper[k] - c.lower[k];
+        if (size > max_size) {
+            max_size = size;
+            max_d = k;
+        }
+    }
+    c.cutAxis = max_d;
+    if (max_d < 0 && zero_volume) ++*zero_volume;
+}
+
+void set_cut_margin(Cell &c) {  // cell.h:123-126 (axis -1 -> axis 0, see header)
+    int a = eff_axis(c);
+    c.cutMarginLeft = c.lower[a];
+    c.cutMarginRight = c.upper[a];
+}
+
+void split(const Cell &p, Cell &left, Cell &right, uint32_t *zero_volume) {  // cell.h:78-100
+    int n_left = (int)std::ceil(p.nLeafCells / 2.0);
+    int n_right = p.nLeafCells - n_left;
+    float cut = get_cut(p);
+    int a = eff_axis(p);
+    left = make_cell(2 * p.id + 1, n_left, p.lower, p.upper);
+    left.upper[a] = cut;
+    left.prevCutAxis = p.cutAxis;
+    right = make_cell(2 * p.id + 2, n_right, p.lower, p.upper);
+    right.lower[a] = cut;
+    right.prevCutAxis = p.cutAxis;
+    // orbit.cpp:240-243
+    set_cut_axis(right, zero_volume);
+    set_cut_margin(right);
+    set_cut_axis(left, zero_volume);
+    set_cut_margin(left);
+}
+
+// orbit.cpp:204-208: ratio = ceil(n/2.0)/n as float; difference = int(float(cl) - float(c)*ratio)
+int convergence(uint32_t count_left, uint32_t count, int32_t n_leaf, int32_t *diff_out) {
+    float ratio = (float)(std::ceil(n_leaf / 2.0) / n_leaf);
+    float prod = (float)count * ratio;
+    float diff_f = (float)count_left - prod;
+    int32_t difference = (int32_t)diff_f;
+    if (diff_out) *diff_out = difference;
+    if (std::abs(difference) < 3) return 0;
+    return difference > 0 ? 1 : -1;
+}
+
+uint32_t count_left(const float *keys, uint64_t begin, uint64_t end, float cut) {  // countLeft.cpp:31-36
+    uint32_t n_left = 0;
+    for (const float *p = keys + begin, *e = keys + end; p < e; ++p) n_left += *p < cut;
+    return n_left;
+}
+
+inline void swap3(float *x, float *y, float *z, uint32_t *perm, int64_t a, int64_t b) {
+    std::swap(x[a], x[b]);
+    std::swap(y[a], y[b]);
+    std::swap(z[a], z[b]);
+    if (perm) std::swap(perm[a], perm[b]);
+}
+
+// partition.cpp:30-52 with the scan clamped at the cell end.
+int64_t hoare(float *x, float *y, float *z, uint32_t *perm, int64_t begin, int64_t end,
+              int axis, float cut, bool final_swap, int *degenerate) {
+    float *key = axis == 0 ? x : (axis == 1 ? y : z);
+    int64_t i = begin - 1, j = end;
+    for (;;) {
+        do {
+            ++i;
+        } while (i < end && key[i] < cut);
+        do {
+            --j;
+        } while (j >= begin && key[j] > cut);
+        if (i >= j) break;
+        swap3(x, y, z, perm, i, j);
+    }
+    if (i < end) {
+        if (final_swap) swap3(x, y, z, perm, i, end - 1);
+        if (degenerate) *degenerate = 0;
+    } else {
+        i = end;
+        if (degenerate) *degenerate = 1;
+    }
+    return i;
+}
+
+// Persistent worker pool: one thread per rank, fork/join per phase (MDL RunService).
+class RankPool {
+   public:
+    explicit RankPool(int n) : n_(n) {
+        for (int r = 1; r < n; ++r) workers_.emplace_back([this, r] { loop(r); });
+    }
+    ~RankPool() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+    void run(const std::function<void(int)> &f) {
+        if (n_ == 1) {
+            f(0);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> g(m_);
+            fn_ = f;
+            pending_ = n_ - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+    }
+
+   private:
+    void loop(int r) {
+        uint64_t seen = 0;
+        for (;;) {
+            std::function<void(int)> f;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                if (stop_) return;
+                f = fn_;
+            }
+            f(r);
+            {
+                std::lock_guard<std::mutex> g(m_);
+                if (--pending_ == 0) done_.notify_one();
+            }
+        }
+    }
+    int n_;
+    std::vector<std::thread> workers_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    std::function<void(int)> fn_;
+    int pending_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+}  // namespace
+
+extern "C" {
+
+uint64_t oracle_draw(uint64_t seed, uint64_t counter) { return draw(seed, counter); }
+
+void oracle_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z, int nthreads) {
+    parallel_chunks(n, nthreads, [=](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i) {
+            x[i] = unit_coord(draw(seed, 3 * i + 0));
+            y[i] = unit_coord(draw(seed, 3 * i + 1));
+            z[i] = unit_coord(draw(seed, 3 * i + 2));
+        }
+    });
+}
+
+void oracle_plummer_clusters(uint64_t seed, float *centres, double *scales) {
+    const uint64_t dom = seed ^ kClusterDomain;
+    for (int k = 0; k < kClusters; ++k) {
+        for (int a = 0; a < 3; ++a) centres[3 * k + a] = unit_coord(draw(dom, 4 * k + a));
+        double u = unit_double(draw(dom, 4 * k + 3));
+        scales[k] = 0.005 * std::pow(10.0, u);  // log-uniform in [0.005, 0.05)
+    }
+}
+
+void oracle_gen_plummer(uint64_t seed, uint64_t n, float *x, float *y, float *z, int nthreads) {
+    float centres[3 * kClusters];
+    double scales[kClusters];
+    oracle_plummer_clusters(seed, centres, scales);
+    const float hi = std::nextafter(0.5f, -1.0f);
+    parallel_chunks(n, nthreads, [&](uint64_t b, uint64_t e) {
+        for (uint64_t i = b; i < e; ++i) {
+            const uint64_t c = i * kPlummerStride;
+            uint64_t sel = draw(seed, c) >> 40;
+            float p[3];
+            if (sel * 10 < 9ull * (1ull << 24)) {  // 90%: Plummer sphere member
+                int k = (int)(draw(seed, c + 1) % kClusters);
+                double w = unit_double(draw(seed, c + 2));
+                w = std::fmax(w, unit_double(draw(seed, c + 3)));
+                w = std::fmax(w, unit_double(draw(seed, c + 4)));
+                // Plummer enclosed mass m(r) = r^3/(r^2+a^2)^1.5; w = m^(1/3) has density 3w^2,
+                // so w = max of three uniforms and r = a w / sqrt(1 - w^2).
+                double r = scales[k] * w / std::sqrt(1.0 - w * w);
+                double v[3] = {1.0, 0.0, 0.0}, q = 1.0;
+                for (int t = 0; t < 19; ++t) {
+                    double u[3];
+                    for (int a = 0; a < 3; ++a)
+                        u[a] = 2.0 * unit_double(draw(seed, c + 5 + 3 * t + a)) - 1.0;
+                    double qq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+                    if (qq > 0.0 && qq <= 1.0) {
+                        v[0] = u[0];
+                        v[1] = u[1];
+                        v[2] = u[2];
+                        q = qq;
+                        break;
+                    }
+                }
+                double s = r / std::sqrt(q);
+                for (int a = 0; a < 3; ++a) {
+                    float f = (float)((double)centres[3 * k + a] + v[a] * s);
+                    p[a] = std::fmin(std::fmax(f, -0.5f), hi);
+                }
+            } else {  // 10%: uniform background
+                for (int a = 0; a < 3; ++a) p[a] = unit_coord(draw(seed, c + 2 + a));
+            }
+            x[i] = p[0];
+            y[i] = p[1];
+            z[i] = p[2];
+        }
+    });
+}
+
+float oracle_get_cut(float margin_left, float margin_right) {
+    Cell c;
+    c.cutMarginLeft = margin_left;
+    c.cutMarginRight = margin_right;
+    return get_cut(c);
+}
+
+int oracle_convergence(uint32_t count_left_v, uint32_t count, int32_t n_leaf_cells,
+                       int32_t *difference_out) {
+    return convergence(count_left_v, count, n_leaf_cells, difference_out);
+}
+
+uint32_t oracle_count_left(const float *keys, uint64_t begin, uint64_t end, float cut) {
+    return count_left(keys, begin, end, cut);
+}
+
+int64_t oracle_hoare(float *x, float *y, float *z, uint32_t *perm, uint64_t begin, uint64_t end,
+                     int axis, float cut, int final_swap, int *degenerate) {
+    return hoare(x, y, z, perm, (int64_t)begin, (int64_t)end, axis, cut, final_swap != 0,
+                 degenerate);
+}
+
+int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t levels,
+                 const float lower[3], const float upper[3], oracle_cell_t *heap,
+                 uint32_t *ranges, uint32_t *perm, uint8_t *iters, int nranks, int make_axis,
+                 oracle_stats_t *stats) {
+    if (!x || !y || !z || !heap || !ranges || d == 0 || (d & (d - 1)) != 0) return -1;
+    if (n >= (1ull << 31)) return -2;
+    uint32_t y_levels = 0;
+    while ((1u << y_levels) < d) ++y_levels;
+    if (levels > y_levels || levels >= ORACLE_MAX_LEVELS) return -3;
+    if (nranks < 1) nranks = 1;
+    if ((uint64_t)nranks > std::max<uint64_t>(n, 1)) nranks = (int)std::max<uint64_t>(n, 1);
+
+    oracle_stats_t st;
+    std::memset(&st, 0, sizeof st);
+    st.nranks = (uint32_t)nranks;
+    const double t0 = now_s();
+
+    const uint64_t heap_size = 2ull * d - 1;
+    std::memset(heap, 0, heap_size * sizeof(Cell));
+    std::memset(ranges, 0, (size_t)nranks * heap_size * 2 * sizeof(uint32_t));
+    if (iters) std::memset(iters, 0, heap_size);
+    if (perm)
+        for (uint64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+
+    // orbit.cpp:74-81
+    Cell root = make_cell(0, (int)d, lower, upper);
+    root.cutAxis = 0;
+    set_cut_margin(root);
+    heap[0] = root;
+
+    // Rank slabs (orbit.cpp:83: N/Threads() particles per rank; the remainder goes to the
+    // last rank here so every particle is owned).
+    struct Rank {
+        uint64_t off, n;
+        uint32_t *rng;
+        std::vector<float> axis_t;
+        std::vector<uint32_t> out;
+    };
+    std::vector<Rank> rk(nranks);
+    for (int r = 0; r < nranks; ++r) {
+        rk[r].off = (n / nranks) * r;
+        rk[r].n = (r == nranks - 1) ? n - rk[r].off : n / nranks;
+        rk[r].rng = ranges + (size_t)r * heap_size * 2;
+        rk[r].rng[0] = 0;
+        rk[r].rng[1] = (uint32_t)rk[r].n;
+        if (make_axis) rk[r].axis_t.resize(rk[r].n + 1);
+    }
+    RankPool pool(nranks);
+
+    std::vector<uint32_t> counts, counts_left;
+    std::vector<std::atomic<uint32_t>> degen(1);
+    degen[0] = 0;
+
+    for (uint32_t l = 1; l <= levels; ++l) {
+        // orbit.cpp:104-111 (getNCellsOnLastLevel() == d for a power-of-two d)
+        const int a = (1 << (l - 1)) - 1;
+        const int b = std::min<int>((int)d, 1 << l) - 2;
+        const int n_cells = b - a + 1;
+        Cell *cells = heap + a;
+        counts.assign(n_cells, 0);
+        counts_left.assign(n_cells, 0);
+
+        if (make_axis) {  // makeAxis.cpp:16-30
+            double ts = now_s();
+            pool.run([&](int r) {
+                Rank &R = rk[r];
+                for (int c = 0; c < n_cells; ++c) {
+                    const Cell &cell = cells[c];
+                    uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
+                    const float *src = (eff_axis(cell) == 0 ? x : eff_axis(cell) == 1 ? y : z) + R.off;
+                    if (en > bg) std::memcpy(R.axis_t.data() + bg, src + bg, (en - bg) * sizeof(float));
+                }
+            });
+            st.t_make_axis_s += now_s() - ts;
+        }
+
+        // count.cpp:14-17 + Combine (sum over ranks)
+        for (int r = 0; r < nranks; ++r)
+            for (int c = 0; c < n_cells; ++c)
+                counts[c] += rk[r].rng[2 * cells[c].id + 1] - rk[r].rng[2 * cells[c].id];
+
+        // orbit.cpp:146-232
+        double ts = now_s();
+        bool found_all = false;
+        int j = 0;
+        while (!found_all && j < 32) {
+            ++j;
+            found_all = true;
+            pool.run([&](int r) {  // countLeft.cpp:16-39 on every rank
+                Rank &R = rk[r];
+                R.out.assign(n_cells, 0);
+                for (int c = 0; c < n_cells; ++c) {
+                    const Cell &cell = cells[c];
+                    if (cell.foundCut) continue;
+                    uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
+                    const float *keys;
+                    if (make_axis) {
+                        keys = R.axis_t.data();
+                    } else {
+                        int ax = eff_axis(cell);
+                        keys = (ax == 0 ? x : ax == 1 ? y : z) + R.off;
+                    }
+                    R.out[c] = count_left(keys, bg, en, get_cut(cell));
+                }
+            });
+            for (int c = 0; c < n_cells; ++c) {  // Combine: elementwise sum
+                uint32_t s = 0;
+                for (int r = 0; r < nranks; ++r) s += rk[r].out[c];
+                counts_left[c] = s;
+            }
+            for (int c = 0; c < n_cells; ++c) {
+                Cell &cell = cells[c];
+                if (cell.foundCut) continue;
+                ++st.cell_counts;
+                st.elements_counted += counts[c];
+                if (iters) iters[cell.id] = (uint8_t)j;
+                int dir = convergence(counts_left[c], counts[c], cell.nLeafCells, nullptr);
+                if (dir == 0) {
+                    cell.foundCut = 1;
+                } else if (dir > 0) {
+                    cell.cutMarginRight = get_cut(cell);
+                    found_all = false;
+                } else {
+                    cell.cutMarginLeft = get_cut(cell);
+                    found_all = false;
+                }
+            }
+        }
+        st.t_count_s += now_s() - ts;
+        st.iterations[l - 1] = (uint32_t)j;
+        for (int c = 0; c < n_cells; ++c)
+            if (!cells[c].foundCut) ++st.unfound_cells;
+
+        // orbit.cpp:235-250
+        for (int c = 0; c < n_cells; ++c) {
+            Cell lc, rc;
+            split(cells[c], lc, rc, &st.zero_volume_cells);
+            heap[lc.id] = lc;
+            heap[rc.id] = rc;
+        }
+
+        // partition.cpp:18-62 on every rank
+        ts = now_s();
+        pool.run([&](int r) {
+            Rank &R = rk[r];
+            uint32_t local_degen = 0;
+            for (int c = 0; c < n_cells; ++c) {
+                const Cell &cell = cells[c];
+                uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
+                int dg = 0;
+                int64_t i = hoare(x + R.off, y + R.off, z + R.off, perm ? perm + R.off : nullptr,
+                                  bg, en, eff_axis(cell), get_cut(cell), true, &dg);
+                local_degen += (uint32_t)dg;
+                const int lcid = 2 * cell.id + 1, rcid = 2 * cell.id + 2;
+                R.rng[2 * lcid] = bg;
+                R.rng[2 * lcid + 1] = (uint32_t)i;
+                R.rng[2 * rcid] = (uint32_t)i;
+                R.rng[2 * rcid + 1] = en;
+            }
+            degen[0] += local_degen;
+        });
+        st.t_partition_s += now_s() - ts;
+        st.levels_built = l;
+    }
+    st.degenerate_cells = degen[0];
+    st.t_total_s = now_s() - t0;
+    if (stats) *stats = st;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+/*
+ * ORB oracle: a CPU restatement of the reference's CPU-only path (orbit mode o=0).
+ *
+ * TEST INFRASTRUCTURE ONLY. Nothing in the product library links, loads or calls this
+ * code; the tests, the smoke check and the benchmark's CPU-baseline leg use it as the
+ * checker and as the timed CPU baseline.
+ *
+ * Reference files followed (paths within andrinr/gpu-load-balance):
+ *   src/cell.h:9-126                 Cell layout, getCut, cut(), setCutAxis, setCutMargin
+ *   src/orbit.cpp:74-81              root cell (cutAxis forced to 0) and cell heap
+ *   src/orbit.cpp:102-111            level slices of the heap
+ *   src/orbit.cpp:146-232            bisection loop, float32 convergence test, 32-iteration cap
+ *   src/orbit.cpp:235-250            split of every cell of the level
+ *   src/services/count.cpp:14-17     cell sizes from the range map
+ *   src/services/makeAxis.cpp:16-30  gather of the cut-axis coordinate (timed baseline only)
+ *   src/services/countLeft.cpp:16-39 count of keys strictly below the cut, found cells skipped
+ *   src/services/partition.cpp:24-62 Hoare partition with the final swap(i, end-1)
+ *   src/services/countLeft.cpp:44-53 rank combine = elementwise sum (multi-rank mode)
+ *
+ * Where the reference reads or writes outside a cell (Hoare scan running off the cell end
+ * when every key is below the cut, including empty cells; src/services/partition.cpp:38,52)
+ * the oracle clamps the scan at the cell end, skips the final swap and counts the cell in
+ * `degenerate_cells`. Where setCutAxis finds no positive extent (cutAxis = -1,
+ * src/cell.h:102-121) the oracle stores -1 in the heap, uses axis 0 for that cell's
+ * count and partition with margins (lower[0], upper[0]), and counts it in
+ * `zero_volume_cells`. The GPU engine implements the same rules.
+ */
+#ifndef ORB_ORACLE_H
+#define ORB_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Byte-for-byte the reference's struct Cell (src/cell.h:9-17): 52 bytes. */
+typedef struct oracle_cell {
+    int32_t id;
+    int32_t nLeafCells;
+    int32_t prevCutAxis;
+    int32_t cutAxis;
+    uint8_t foundCut;
+    uint8_t pad_[3];
+    float cutMarginLeft;
+    float cutMarginRight;
+    float lower[3];
+    float upper[3];
+} oracle_cell_t;
+
+#define ORACLE_MAX_LEVELS 40
+
+typedef struct oracle_stats {
+    uint32_t levels_built;
+    uint32_t iterations[ORACLE_MAX_LEVELS]; /* bisection sweeps (j) per level */
+    uint64_t cell_counts;                   /* count-left evaluations (cell x iteration) */
+    uint64_t elements_counted;              /* keys read by count-left over the build */
+    uint32_t degenerate_cells;              /* Hoare scan clamped at the cell end */
+    uint32_t zero_volume_cells;             /* setCutAxis found no positive extent */
+    uint32_t unfound_cells;                 /* bisection stopped by the 32-sweep cap */
+    uint32_t nranks;
+    double t_make_axis_s;
+    double t_count_s;
+    double t_partition_s;
+    double t_total_s;
+} oracle_stats_t;
+
+/* Seeded generators shared bit-for-bit with the engine's device generator. */
+uint64_t oracle_draw(uint64_t seed, uint64_t counter);
+void oracle_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z, int nthreads);
+void oracle_plummer_clusters(uint64_t seed, float *centres /*64*3*/, double *scales /*64*/);
+void oracle_gen_plummer(uint64_t seed, uint64_t n, float *x, float *y, float *z, int nthreads);
+
+/* Reference arithmetic primitives. */
+float oracle_get_cut(float margin_left, float margin_right);
+/* Returns 0 = found, +1 = move the right margin to the cut, -1 = move the left margin. */
+int oracle_convergence(uint32_t count_left, uint32_t count, int32_t n_leaf_cells,
+                       int32_t *difference_out);
+uint32_t oracle_count_left(const float *keys, uint64_t begin, uint64_t end, float cut);
+/* Hoare partition of [begin,end) of x,y,z (and perm if non-null) on `axis` at `cut`.
+ * Returns the split index i; *degenerate set to 1 when the scan was clamped. */
+int64_t oracle_hoare(float *x, float *y, float *z, uint32_t *perm, uint64_t begin,
+                     uint64_t end, int axis, float cut, int final_swap, int *degenerate);
+
+/*
+ * Full ORB build, in place on x,y,z (the particle order after the build is the
+ * reference's partitioned order).
+ *   d        leaf cells, a power of two; heap holds 2d-1 cells, ranges 2*(2d-1) uint32
+ *   levels   split levels to run: log2(d) gives d leaves, log2(d)-1 is the reference's
+ *            own loop bound (src/orbit.cpp:102)
+ *   perm     optional: original index of the particle at each position
+ *   iters    optional: bisection iterations spent on each heap cell
+ *   nranks   1 = canonical single-rank oracle. >1 = the reference's MDL semantics: the
+ *            particles are split into nranks contiguous slabs, per-cell counts are summed
+ *            over ranks and each rank partitions its own slab (run on nranks threads).
+ *            `ranges` then holds nranks consecutive range maps.
+ *   make_axis  1 = also perform the per-level cut-axis gather the reference performs
+ *            (src/services/makeAxis.cpp); results are identical, only timing changes.
+ * Returns 0 on success, a negative value on invalid arguments.
+ */
+int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t levels,
+                 const float lower[3], const float upper[3], oracle_cell_t *heap,
+                 uint32_t *ranges, uint32_t *perm, uint8_t *iters, int nranks,
+                 int make_axis, oracle_stats_t *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,196 @@
+"""GPU parity of the engine (through the C ABI) against the CPU oracle.
+
+Bit-exact on every output: the cell heap (cuts, margins, found flags, boxes, axes), the
+range map, the permutation (particle -> position) and the reordered coordinates."""
+import numpy as np
+import pytest
+
+from helpers import tree_properties
+
+pytestmark = pytest.mark.gpu
+
+
+def first_heap_diff(a, b):
+    for i in range(len(a)):
+        if a[i].tobytes() != b[i].tobytes():
+            return i, a[i], b[i]
+    return None
+
+
+def assert_same(res, ref, gx, gy, gz):
+    d = first_heap_diff(res.heap, ref.heap)
+    assert d is None, f"heap differs first at cell {d[0]}:\n gpu {d[1]}\n cpu {d[2]}"
+    assert np.array_equal(res.ranges, ref.ranges[0]), "range map differs"
+    assert np.array_equal(res.perm, ref.perm), "particle order differs"
+    assert np.array_equal(gx, ref.x) and np.array_equal(gy, ref.y) and np.array_equal(gz, ref.z)
+
+
+def run_both(ctx, oracle, x, y, z, d, levels=0, **kw):
+    ref = oracle.build_tree(x, y, z, d, levels=(levels or None), **kw)
+    gx, gy, gz = x.copy(), y.copy(), z.copy()
+    res = ctx.build(gx, gy, gz, d, levels=levels, **kw)
+    assert_same(res, ref, gx, gy, gz)
+    assert res.info["degenerate_cells"] == ref.stats["degenerate_cells"]
+    assert res.info["unfound_cells"] == ref.stats["unfound_cells"]
+    assert res.info["zero_volume_cells"] == ref.stats["zero_volume_cells"]
+    return res, ref
+
+
+@pytest.mark.parametrize("kind", ["uniform", "plummer"])
+def test_generator_bit_exact(ctx, engine, oracle, kind):
+    n = (1 << 20) + 37
+    gen = oracle.gen_uniform if kind == "uniform" else oracle.gen_plummer
+    x, y, z = gen(42, n)
+    k = engine.ORB_GEN_UNIFORM if kind == "uniform" else engine.ORB_GEN_PLUMMER
+    gx, gy, gz = ctx.generate_host(k, 42, n)
+    assert np.array_equal(gx, x) and np.array_equal(gy, y) and np.array_equal(gz, z)
+
+
+@pytest.mark.parametrize("n,d,seed", [(1 << 12, 1 << 4, 1), (1 << 16, 1 << 8, 2),
+                                      ((1 << 16) + 123, 1 << 9, 3), (50000, 1 << 12, 4)])
+def test_uniform_parity(ctx, oracle, n, d, seed):
+    x, y, z = oracle.gen_uniform(seed, n)
+    run_both(ctx, oracle, x, y, z, d)
+
+
+def test_config1_parity(ctx, oracle):
+    """2^20 uniform particles, 2^10 leaves (the reference's CPU-runnable case)."""
+    x, y, z = oracle.gen_uniform(2024, 1 << 20)
+    res, ref = run_both(ctx, oracle, x, y, z, 1 << 10)
+    assert res.info["max_iterations"] == max(ref.stats["iterations"])
+
+
+@pytest.mark.parametrize("n,d,seed", [(1 << 16, 1 << 10, 5), (1 << 18, 1 << 12, 6)])
+def test_plummer_parity(ctx, oracle, n, d, seed):
+    x, y, z = oracle.gen_plummer(seed, n)
+    run_both(ctx, oracle, x, y, z, d)
+
+
+def test_tie_heavy_parity(ctx, oracle):
+    """Coordinates on a 64-value grid: most cuts land on keys, Hoare tie placement decides
+    membership."""
+    rng = np.random.default_rng(7)
+    n = 1 << 17
+    x, y, z = ((rng.integers(0, 64, n).astype(np.float32) / np.float32(64) - np.float32(0.5))
+               for _ in range(3))
+    res, ref = run_both(ctx, oracle, x, y, z, 1 << 10)
+    assert ref.stats["unfound_cells"] > 0  # the grid defeats the bisection somewhere
+
+
+def test_small_and_degenerate_cells(ctx, oracle):
+    rng = np.random.default_rng(8)
+    for n in (0, 1, 2, 3, 5, 7, 17, 100):
+        for d in (1, 2, 4, 16):
+            x, y, z = (rng.random(n).astype(np.float32) - np.float32(0.5) for _ in range(3))
+            run_both(ctx, oracle, x, y, z, d)
+
+
+def test_duplicates_nan_out_of_box(ctx, oracle):
+    n = 4096
+    same = np.full(n, 0.25, np.float32)
+    run_both(ctx, oracle, same, same.copy(), same.copy(), 8)
+    rng = np.random.default_rng(9)
+    x = rng.random(n).astype(np.float32) - np.float32(0.5)
+    x[rng.integers(0, n, 200)] = np.nan
+    y = rng.random(n).astype(np.float32) * np.float32(4) - np.float32(2)  # out of the box
+    z = np.round(rng.random(n).astype(np.float32) * 8) / np.float32(8) - np.float32(0.5)
+    run_both(ctx, oracle, x, y, z, 64)
+
+
+def test_reference_level_bound(ctx, oracle):
+    """levels = log2(d)-1 is the reference driver's own loop (d/2 leaves)."""
+    x, y, z = oracle.gen_uniform(10, 1 << 15)
+    run_both(ctx, oracle, x, y, z, 1 << 8, levels=7)
+
+
+def test_custom_box(ctx, oracle):
+    x, y, z = oracle.gen_uniform(12, 1 << 14)
+    x = x * np.float32(3)
+    run_both(ctx, oracle, x, y, z, 1 << 6, lower=(-1.5, -0.5, -0.5), upper=(1.5, 0.5, 0.5))
+
+
+def test_device_pointers(ctx, oracle):
+    torch = pytest.importorskip("torch")
+    n, d = 1 << 18, 1 << 10
+    x, y, z = oracle.gen_uniform(13, n)
+    ref = oracle.build_tree(x, y, z, d)
+    tx, ty, tz = (torch.from_numpy(a.copy()).cuda() for a in (x, y, z))
+    tp = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    res = ctx.build(tx, ty, tz, d, perm=tp, device_pointers=True)
+    assert res.heap.tobytes() == ref.heap.tobytes()
+    assert np.array_equal(res.ranges, ref.ranges[0])
+    assert np.array_equal(tp.cpu().numpy().view(np.uint32), ref.perm)
+    assert np.array_equal(tx.cpu().numpy(), ref.x)
+
+
+def test_service_layer(ctx, engine, oracle):
+    """orb_count / orb_count_left / orb_partition reproduce the reference's services when
+    driven by a host-side master loop (src/orbit.cpp:102-275)."""
+    n, d = 1 << 15, 1 << 5
+    x, y, z = oracle.gen_uniform(14, n)
+    ref = oracle.build_tree(x, y, z, d)
+    heap_cells = 2 * d - 1
+    ctx.load_particles(x, y, z, heap_cells)
+    heap = np.zeros(heap_cells, engine.CELL_DTYPE)
+    heap[0]["nLeafCells"] = d
+    heap[0]["prevCutAxis"] = -1
+    heap[0]["cutAxis"] = 0
+    heap[0]["lower"] = (-0.5, -0.5, -0.5)
+    heap[0]["upper"] = (0.5, 0.5, 0.5)
+    heap[0]["cutMarginLeft"], heap[0]["cutMarginRight"] = -0.5, 0.5
+    levels = d.bit_length() - 1
+    for l in range(1, levels + 1):
+        a, b = (1 << (l - 1)) - 1, (1 << l) - 2
+        cells = heap[a:b + 1].copy()
+        counts = ctx.count(cells)
+        left = np.zeros(len(cells), np.uint32)
+        for _ in range(32):
+            ctx.count_left(cells, left)
+            done = True
+            for i in range(len(cells)):
+                if cells[i]["foundCut"]:
+                    continue
+                r, _ = oracle.convergence(int(left[i]), int(counts[i]), int(cells[i]["nLeafCells"]))
+                cut = oracle.get_cut(float(cells[i]["cutMarginLeft"]), float(cells[i]["cutMarginRight"]))
+                if r == 0:
+                    cells[i]["foundCut"] = 1
+                elif r > 0:
+                    cells[i]["cutMarginRight"] = cut
+                    done = False
+                else:
+                    cells[i]["cutMarginLeft"] = cut
+                    done = False
+            if done:
+                break
+        heap[a:b + 1] = cells
+        # split on the host from the oracle's heap (the services do not split)
+        for c in range(a, b + 1):
+            heap[2 * c + 1] = ref.heap[2 * c + 1]
+            heap[2 * c + 2] = ref.heap[2 * c + 2]
+        ctx.partition(cells)
+    assert heap.tobytes() == ref.heap.tobytes()
+    assert np.array_equal(ctx.get_ranges(heap_cells), ref.ranges[0])
+    sx, sy, sz, sp = ctx.store_particles()
+    assert np.array_equal(sp, ref.perm) and np.array_equal(sx, ref.x)
+
+
+def test_large_parity(ctx, oracle):
+    """2^24 particles, 2^13 leaves: bit-exact against the oracle."""
+    x, y, z = oracle.gen_uniform(99, 1 << 24)
+    run_both(ctx, oracle, x, y, z, 1 << 13)
+
+
+def test_headline_properties(ctx, oracle, engine):
+    """2^27 particles, 2^16 leaves: size-independent properties of the device build."""
+    n, d = 1 << 27, 1 << 16
+    x, y, z = ctx.generate_host(engine.ORB_GEN_UNIFORM, 2027, n)
+    res = ctx.build(x, y, z, d)
+    tree_properties(x, y, z, res.heap, res.ranges, n, d, 16)
+    perm = res.perm
+    seen = np.zeros(n, np.bool_)
+    seen[perm] = True
+    assert seen.all()
+    leaves = res.ranges[(1 << 16) - 1:]
+    sizes = leaves[:, 1].astype(np.int64) - leaves[:, 0]
+    assert sizes.min() >= 2048 - 64 and sizes.max() <= 2048 + 64

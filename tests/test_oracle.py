@@ -1,0 +1,264 @@
+"""CPU tests of the oracle: pinned against the reference's own worked example, the
+reference's float32 arithmetic, the literal Hoare loop, and its own committed digests."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import tree_properties
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _doc():
+    with open(os.path.join(GOLDEN, "doc_example.json")) as f:
+        return json.load(f)
+
+
+def _arrays(rec):
+    x = np.array(rec["x"], np.float32)
+    y = np.array(rec["y"], np.float32)
+    ids = np.array(rec["id"], np.uint32)
+    return x, y, ids
+
+
+def test_doc_example_x_cut(oracle):
+    """documentation/particles10.csv -> particles11.csv (cut x = 0.65)."""
+    doc = _doc()
+    x, y, ids = _arrays(doc["initial"])
+    ex, ey, eids = _arrays(doc["after_x_cut"])
+    # The thesis tables show the Hoare loop without the final swap(i, end-1).
+    z = np.zeros_like(x)
+    xx, yy, zz, pp = x.copy(), y.copy(), z.copy(), ids.copy()
+    i, dg = oracle.hoare(xx, yy, zz, 0, doc["x_cut"], final_swap=False, perm=pp)
+    assert dg == 0 and i == 4
+    assert np.array_equal(pp, eids) and np.array_equal(xx, ex) and np.array_equal(yy, ey)
+    # The reference code (partition.cpp:52) adds swap(i, end-1): same membership.
+    xx, yy, zz, pp = x.copy(), y.copy(), z.copy(), ids.copy()
+    i2, _ = oracle.hoare(xx, yy, zz, 0, doc["x_cut"], final_swap=True, perm=pp)
+    assert i2 == 4
+    assert set(pp[:4]) == set(eids[:4]) and set(pp[4:]) == set(eids[4:])
+    assert list(pp) == list(eids[:4]) + [eids[6], eids[5], eids[4]]
+
+
+def test_doc_example_y_cut(oracle):
+    """particles11.csv -> particles12.csv (cut y = 0.55 on the first four rows)."""
+    doc = _doc()
+    x, y, ids = _arrays(doc["after_x_cut"])
+    ex, ey, eids = _arrays(doc["after_y_cut"])
+    b, e = doc["y_cut_cell"]
+    z = np.zeros_like(x)
+    xx, yy, zz, pp = x.copy(), y.copy(), z.copy(), ids.copy()
+    i, dg = oracle.hoare(xx, yy, zz, 1, doc["y_cut"], begin=b, end=e, final_swap=False, perm=pp)
+    assert dg == 0 and i == 2
+    assert np.array_equal(pp, eids) and np.array_equal(yy, ey)
+    xx, yy, zz, pp = x.copy(), y.copy(), z.copy(), ids.copy()
+    i2, _ = oracle.hoare(xx, yy, zz, 1, doc["y_cut"], begin=b, end=e, final_swap=True, perm=pp)
+    assert i2 == 2 and set(pp[:2]) == set(eids[:2]) and set(pp[2:4]) == set(eids[2:4])
+
+
+def test_doc_example_cell_count(oracle):
+    """notes.tex:544: for d=3 and 7 particles the left cell holds ceil-based 4 particles;
+    with the code's rule ratio = ceil(3/2)/3 (orbit.cpp:204) the cut is accepted when
+    |int(cl - 7*ratio)| < 3."""
+    r, diff = oracle.convergence(4, 7, 3)
+    assert r == 0 and diff == -0
+    r, diff = oracle.convergence(0, 7, 2)   # 0 - 3.5 -> int(-3.5) = -3
+    assert (r, diff) == (-1, -3)
+    r, diff = oracle.convergence(1, 7, 2)   # 1 - 3.5 = -2.5 -> -2 -> found
+    assert (r, diff) == (0, -2)
+
+
+@pytest.mark.parametrize(
+    "cl,c,expect",
+    [
+        # above 2^24 the uint->float conversions round (orbit.cpp:205)
+        ((1 << 26) + 4, 1 << 27, (0, 0)),        # 2^26+4 rounds (to even) to 2^26
+        ((1 << 26) + 5, 1 << 27, (1, 8)),        # rounds up to 2^26+8
+        ((1 << 26) - 3, 1 << 27, (-1, -4)),      # spacing 4 below 2^26
+        # 2^26+6 -> 2^26+8 (spacing 8), halved 2^25+4; 2^25+2 ties to even -> 2^25
+        ((1 << 25) + 2, (1 << 26) + 6, (-1, -4)),
+        ((1 << 25) + 6, (1 << 26) + 6, (1, 4)),   # 2^25+6 ties to even -> 2^25+8
+        (10, 20, (0, 0)),
+        (13, 20, (1, 3)),
+        (7, 20, (-1, -3)),
+    ],
+)
+def test_convergence_float_semantics(oracle, cl, c, expect):
+    assert oracle.convergence(cl, c, 2) == expect
+
+
+def test_get_cut_exact(oracle):
+    f32 = np.float32
+    assert oracle.get_cut(-0.5, 0.5) == 0.0
+    assert oracle.get_cut(-0.5, 0.0) == -0.25
+    # (R + L) is rounded in float32 before the halving (cell.h:75)
+    a, b = f32(1.0), f32(2.0 ** -24)
+    expect = f32(np.float64(f32(a + b)) / 2.0)
+    assert oracle.get_cut(float(b), float(a)) == float(expect)
+    # halving of a subnormal sum rounds to nearest even
+    t = f32(np.float32(2.0 ** -149) * 3)
+    assert oracle.get_cut(float(t), 0.0) == float(f32(np.float64(t) / 2.0))
+
+
+def _parallel_hoare(keys, cut):
+    """The parallel characterisation used by the GPU partition (numpy, small sizes)."""
+    n = len(keys)
+    ge = ~(keys < cut)
+    le = ~(keys > cut)
+    f = np.concatenate([[0], np.cumsum(ge)])
+    g = np.concatenate([np.cumsum(le[::-1])[::-1], [0]])
+    s = int(np.max(np.minimum(f, g)))
+    L = np.nonzero(ge)[0]
+    R = np.nonzero(le)[0][::-1]
+    i = min(L[s] if s < len(L) else n, R[s - 1] if s >= 1 else n)
+    p = np.arange(n)
+    p[L[:s]] = R[:s]
+    p[R[:s]] = L[:s]
+    if i < n:
+        p[[i, n - 1]] = p[[n - 1, i]]
+    return i, p, int(i >= n)
+
+
+def test_parallel_hoare_matches_loop(oracle):
+    rng = np.random.default_rng(1234)
+    for _ in range(4000):
+        n = int(rng.integers(0, 48))
+        span = int(rng.integers(1, 7))
+        keys = rng.integers(0, span, n).astype(np.float32)
+        if rng.random() < 0.1 and n:
+            keys[rng.integers(0, n)] = np.nan
+        cut = np.float32(rng.integers(-1, span + 1) - 0.5 * rng.integers(0, 2))
+        x = keys.copy()
+        y = np.zeros(n, np.float32)
+        z = np.zeros(n, np.float32)
+        perm = np.arange(n, dtype=np.uint32)
+        i, dg = oracle.hoare(x, y, z, 0, float(cut), perm=perm)
+        i2, p, dg2 = _parallel_hoare(keys, cut)
+        assert (i, dg) == (i2, dg2)
+        assert np.array_equal(perm, p.astype(np.uint32))
+
+
+def test_oracle_digests(oracle):
+    with open(os.path.join(GOLDEN, "oracle_builds.json")) as f:
+        cases = json.load(f)
+    checked = 0
+    for c in cases:
+        gen = oracle.gen_uniform if c["kind"] == "uniform" else oracle.gen_plummer
+        x, y, z = gen(c["seed"], c["n"])
+        hin = hashlib.sha256()
+        for a in (x, y, z):
+            hin.update(a.tobytes())
+        if hin.hexdigest() != c["input_sha256"]:
+            # only the Plummer generator uses libm (pow for the 64 scale radii)
+            assert c["kind"] == "plummer", "uniform generator changed"
+            continue
+        r = oracle.build_tree(x, y, z, c["d"])
+        h = hashlib.sha256()
+        for a in (r.heap, r.ranges, r.perm, r.x, r.y, r.z):
+            h.update(a.tobytes())
+        assert h.hexdigest() == c["build_sha256"], f"oracle result changed for {c}"
+        checked += 1
+    assert checked >= 2
+
+
+def test_generator_uniform_grid(oracle):
+    x, y, z = oracle.gen_uniform(5, 1 << 16)
+    for a in (x, y, z):
+        assert a.min() >= -0.5 and a.max() < 0.5
+        k = (a.astype(np.float64) + 0.5) * (1 << 24)
+        assert np.all(k == np.floor(k))
+    # counter-based: a prefix of a larger draw is the smaller draw
+    x2, _, _ = oracle.gen_uniform(5, 1 << 10)
+    assert np.array_equal(x2, x[: 1 << 10])
+
+
+def test_generator_plummer_in_box(oracle):
+    x, y, z = oracle.gen_plummer(9, 1 << 16)
+    hi = np.nextafter(np.float32(0.5), np.float32(-1))
+    for a in (x, y, z):
+        assert a.min() >= -0.5 and a.max() <= hi
+    # clustered: far from uniform occupancy of an 8^3 grid
+    idx = ((np.stack([x, y, z], 1) + 0.5) * 8).astype(int).clip(0, 7)
+    occ = np.bincount(idx[:, 0] * 64 + idx[:, 1] * 8 + idx[:, 2], minlength=512)
+    assert occ.max() > 8 * occ.mean()
+
+
+@pytest.mark.parametrize("kind,n,d", [("uniform", 1 << 14, 1 << 6), ("plummer", 1 << 15, 1 << 8)])
+def test_oracle_tree_properties(oracle, kind, n, d):
+    gen = oracle.gen_uniform if kind == "uniform" else oracle.gen_plummer
+    x, y, z = gen(11, n)
+    r = oracle.build_tree(x, y, z, d)
+    levels = d.bit_length() - 1
+    tree_properties(r.x, r.y, r.z, r.heap, r.ranges[0], n, d, levels)
+    assert np.array_equal(np.sort(r.perm), np.arange(n, dtype=np.uint32))
+    assert np.array_equal(r.x, x[r.perm])
+    leaves = r.ranges[0][(1 << levels) - 1:]
+    sizes = leaves[:, 1].astype(np.int64) - leaves[:, 0]
+    assert sizes.sum() == n
+    if kind == "uniform":
+        assert sizes.max() - sizes.min() <= 4 * levels
+
+
+def test_reference_level_bound_is_prefix(oracle):
+    """levels = log2(d)-1 (the reference's loop bound) is the exact prefix of the full build."""
+    x, y, z = oracle.gen_uniform(3, 1 << 13)
+    d = 1 << 6
+    full = oracle.build_tree(x, y, z, d)
+    part = oracle.build_tree(x, y, z, d, levels=5)
+    k = (1 << 6) - 1  # cells of depth <= 5
+    # cells of depth < 5 are identical; depth-5 cells were split in the full build only
+    assert part.heap[: (1 << 5) - 1].tobytes() == full.heap[: (1 << 5) - 1].tobytes()
+    assert np.array_equal(part.ranges[0][:k], full.ranges[0][:k])
+    hd = part.heap[(1 << 5) - 1: k].copy()
+    fd = full.heap[(1 << 5) - 1: k].copy()
+    for f in ("id", "nLeafCells", "prevCutAxis", "cutAxis", "lower", "upper"):
+        assert np.array_equal(hd[f], fd[f])
+    assert np.all(part.heap[k:]["nLeafCells"] == 0)
+
+
+def test_multirank_equals_single_rank_without_ties(oracle):
+    rng = np.random.default_rng(5)
+    n = 1 << 14
+    x, y, z = (rng.random(n, dtype=np.float64).astype(np.float32) - np.float32(0.5) for _ in range(3))
+    one = oracle.build_tree(x, y, z, 1 << 6)
+    many = oracle.build_tree(x, y, z, 1 << 6, nranks=4, make_axis=True)
+    # cuts are decided on summed counts: same heap unless a tie sits on a cut
+    same = one.heap.tobytes() == many.heap.tobytes()
+    cuts = oracle.cut_of(one.heap[: (1 << 6) - 1])
+    ties = any(np.isin(cuts, a).any() for a in (x, y, z))
+    assert same or ties
+    # per-rank range maps add up to the single-rank cell sizes
+    tot = (many.ranges[:, :, 1].astype(np.int64) - many.ranges[:, :, 0]).sum(0)
+    sizes = one.ranges[0][:, 1].astype(np.int64) - one.ranges[0][:, 0]
+    if same:
+        assert np.array_equal(tot, sizes)
+
+
+def test_edge_cases(oracle):
+    lo, hi = (-0.5,) * 3, (0.5,) * 3
+    # empty input: every cell found at once, every partition clamped
+    e = np.zeros(0, np.float32)
+    r = oracle.build_tree(e, e, e, 4)
+    assert r.stats["degenerate_cells"] == 3 and np.all(r.ranges[0] == 0)
+    # one particle
+    one = np.array([0.1], np.float32)
+    r = oracle.build_tree(one, one, one, 2)
+    assert r.heap[0]["foundCut"] == 1
+    # all keys equal: never found, 32 iterations, every split clamps or ties
+    n = 64
+    same = np.full(n, 0.25, np.float32)
+    r = oracle.build_tree(same, same, same, 2)
+    assert r.stats["unfound_cells"] == 1 and r.stats["iterations"][0] == 32
+    # NaN keys behave as ties in Hoare and never count as left
+    x = np.array([np.nan, -0.3, 0.2, np.nan, 0.4, -0.1], np.float32)
+    r = oracle.build_tree(x, x.copy(), x.copy(), 2)
+    assert r.stats["levels_built"] == 1
+    # out-of-box particles are handled by the same comparisons
+    xo = np.array([-3.0, 2.0, 0.1, -0.2, 0.3, 5.0, -7.0, 0.0], np.float32)
+    r = oracle.build_tree(xo, xo.copy(), xo.copy(), 4, lower=lo, upper=hi)
+    assert r.stats["levels_built"] == 2
+    with pytest.raises(ValueError):
+        oracle.build_tree(x, x, x, 3)  # not a power of two
