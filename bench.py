@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""ORB build benchmark on GB300: 2^27 uniform float32 particles into 2^16 leaf cells.
+
+One step = one ORB build (orb_build through the C ABI) of the whole particle set, preceded
+by a device-to-device restore of the unpartitioned input (the build partitions in place).
+
+  value      particles/s with inputs resident in HBM (restore + build per step)
+  e2e        particles/s through orb_build with pinned HOST buffers: H2D of x,y,z, build,
+             D2H of the reordered x,y,z, the permutation, the cell heap and the range map
+  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time (live, on the
+             engine's stream) against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle with the reference's MDL semantics (one rank per host core,
+             per-cell counts summed, per-rank Hoare partition) on the same workload
+
+--impl reference times that CPU implementation alone (rank 0), as the reference arm.
+With torchrun (N>1) every rank builds its own replica on its own GPU (the path has no
+data exchange on one GPU per box): value sums the particles of all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "gpu-load-balance_gb300")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG_DIR)
+
+N_PARTICLES = 1 << 27
+LEAVES = 1 << 16
+SEED = 20270
+METRIC = "orb_build_particles_per_s"
+UNIT = "particles/s"
+WORKLOAD = "plain ORB, 2^27 uniform float32 particles in [-0.5,0.5)^3, 2^16 leaf cells"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.rows = []
+        self.proc = None
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        if gpu_id is not None:
+            cmd += ["-i", gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.mark = None
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append((time.perf_counter(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        sel = [r for (t, r) in self.rows if t0 <= t <= t1] or [r for (_, r) in self.rows]
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in sel if num(r[1]) is not None]
+        mx = [num(r[2]) for r in sel if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in sel:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sel)}
+
+
+def gpu_id_for(local_rank: int):
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd:
+        ids = [s.strip() for s in cvd.split(",") if s.strip()]
+        if local_rank < len(ids):
+            return ids[local_rank]
+    return str(local_rank)
+
+
+# ------------------------------------------------------------------------------------------
+# CPU implementation (the oracle with the reference's MDL semantics)
+# ------------------------------------------------------------------------------------------
+def cpu_build_probe(n: int, d: int, threads: int):
+    sys.path.insert(0, ORACLE_DIR)
+    import oracle as O  # the checker; used here only as the timed CPU baseline
+    O.build()
+    x, y, z = O.gen_uniform(SEED, n, nthreads=threads)
+    t = time.perf_counter()
+    r = O.build_tree(x, y, z, d, nranks=threads, make_axis=True, copy=False, want_perm=False)
+    return time.perf_counter() - t, r.stats
+
+
+def cpu_sample_size(budget_s: float, steps: int, threads: int):
+    """Largest (n, d) with the workload's particles-per-leaf whose run fits the budget."""
+    n, d = N_PARTICLES, LEAVES
+    t_probe, _ = cpu_build_probe(n >> 5, d >> 5, threads)
+    per_step = t_probe * 32 * 1.15  # levels grow by 5 at full size
+    while per_step * steps > budget_s and n > (1 << 20):
+        n >>= 1
+        d >>= 1
+        per_step /= 2
+    return n, d
+
+
+def run_cpu(steps: int, warmup: int, budget_s: float):
+    threads = os.cpu_count() or 1
+    n, d = cpu_sample_size(budget_s, steps + warmup, threads)
+    times = []
+    stats = None
+    for i in range(warmup + steps):
+        t, stats = cpu_build_probe(n, d, threads)
+        if i >= warmup:
+            times.append(t)
+    total = sum(times)
+    value = n * len(times) / total
+    sample = (f"oracle with MDL semantics ({threads} ranks = host threads, makeAxis gather on), "
+              f"{n} particles / {d} leaves per step (same particles per leaf as the workload), "
+              f"{len(times)} steps")
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+            "ms_per_step": 1e3 * total / len(times), "phase_s": {k: stats[k] for k in
+            ("t_make_axis_s", "t_count_s", "t_partition_s", "t_total_s")}}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    cpu = run_cpu(args.steps, args.warmup, budget_s=150.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cpu["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform)",
+        "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "leaves": LEAVES,
+                   "l2": "inputs 1.5 GB > L2"},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def gpu_arm(args):
+    import numpy as np
+    import torch
+
+    import orb_gb300 as E
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    E.build()
+    n, d = args.particles, args.leaves
+    ctx = E.Context(local, reserve_particles=n, reserve_leaves=d)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # inputs generated on the device by the engine's seeded generator
+    x0, y0, z0 = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    ctx.generate(E.ORB_GEN_UNIFORM, SEED + rank, n, x0, y0, z0, device_pointers=True)
+    x, y, z = (torch.empty_like(x0) for _ in range(3))
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def step():
+        x.copy_(x0)
+        y.copy_(y0)
+        z.copy_(z0)
+        torch.cuda.synchronize(dev)
+        return ctx.build(x, y, z, d, perm=perm, device_pointers=True)
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(gpu_id_for(local))
+    time.sleep(0.5)
+    ctx.profile_reset(timing=True)
+    barrier()
+    torch.cuda.synchronize(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    tw0 = time.perf_counter()
+    ev0.record()
+    infos = []
+    for _ in range(args.steps):
+        infos.append(step().info)
+    ev1.record()
+    torch.cuda.synchronize(dev)
+    tw1 = time.perf_counter()
+    barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    prof = ctx.profile()
+    if world > 1:
+        t = torch.tensor([ms_total])
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = n * world * args.steps / (ms_total / 1e3)
+
+    # end to end through the C ABI with pinned host buffers
+    hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
+    hp = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    hx.copy_(x0.cpu()); hy.copy_(y0.cpu()); hz.copy_(z0.cpu())
+    src = [t.numpy().copy() for t in (hx, hy, hz)]
+    nx, ny, nz, npp = hx.numpy(), hy.numpy(), hz.numpy(), hp.numpy().view(np.uint32)
+    e2e_times = []
+    te0 = time.perf_counter()
+    for i in range(args.warmup + args.steps):
+        for a, s in zip((nx, ny, nz), src):
+            np.copyto(a, s)
+        t = time.perf_counter()
+        ctx.build(nx, ny, nz, d, perm=npp)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t)
+    te1 = time.perf_counter()
+    e2e_s = sum(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s])
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = n * world * len(e2e_times) / e2e_s
+    clocks.stop()
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peak()
+    timed = {k: v for k, v in prof.items() if v["total_ms"] > 0}
+    dom = max(timed, key=lambda k: timed[k]["total_ms"])
+    dk = timed[dom]
+    achieved = dk["bytes"] / (dk["total_ms"] / 1e3) / 1e9
+    kern_ms_total = sum(v["total_ms"] for v in timed.values())
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+        "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+        "traffic": None,
+        "bytes_per_launch": dk["bytes"] / dk["launches"],
+        "ms_per_launch": dk["total_ms"] / dk["launches"],
+        "share_of_kernel_time": round(dk["total_ms"] / kern_ms_total, 4),
+    }
+    kernels = {k: {"launches": v["launches"] // args.steps,
+                   "ms": round(v["total_ms"] / args.steps, 4),
+                   "GBps": round(v["bytes"] / (v["total_ms"] / 1e3) / 1e9, 1) if v["total_ms"] else None}
+               for k, v in prof.items()}
+    launches = sum(v["launches"] for v in prof.values())
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = run_cpu(1, 0, budget_s=40.0)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    heap_bytes = (2 * d - 1) * 52
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform, engine generator)",
+        "config": {"workload": WORKLOAD, "particles": n, "leaves": d, "levels": 16,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs 1.5 GB > 129 MB L2 (no flush needed)",
+                   "step": "d2d restore of x,y,z + orb_build (device pointers)"},
+        "build_ms_device": statistics.median(i["device_ms"] for i in infos),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
+                "d2h_bytes_per_step": 16 * n + heap_bytes + 8 * (2 * d - 1),
+                "ms_per_step": 1e3 * e2e_s / len(e2e_times)},
+        "roofline": roofline,
+        "kernels_per_step": kernels,
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(tw0, te1),
+        "bisection_passes_per_build": infos[-1]["count_passes"],
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--particles", type=int, default=N_PARTICLES)
+    ap.add_argument("--leaves", type=int, default=LEAVES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

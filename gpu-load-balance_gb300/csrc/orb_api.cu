@@ -8,10 +8,12 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "orb_internal.cuh"
@@ -78,6 +80,18 @@ struct orb_ctx {
     bool loaded = false;
     uint64_t loaded_n = 0;
     uint32_t loaded_cells = 0;
+
+    // profiling: launch counts always; CUDA-event durations when `prof_timing` is set
+    bool prof_timing = false;
+    uint64_t launches[kNumKernels] = {};
+    double prof_ms[kNumKernels] = {};
+    double prof_bytes[kNumKernels] = {};
+    struct Rec {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> ev_pool;
 };
 
 namespace {
@@ -168,13 +182,61 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
 
 int pass_grid(orb_ctx *ctx) { return ctx->num_sms * 8; }
 
+cudaEvent_t take_event(orb_ctx *ctx) {
+    if (!ctx->ev_pool.empty()) {
+        cudaEvent_t e = ctx->ev_pool.back();
+        ctx->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+// Launches one level kernel on the context stream; counted, and event-timed if enabled.
+void run_kernel(orb_ctx *ctx, Kernel k, const Level &v, int grid, int arg = 0) {
+    ctx->launches[k] += 1;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (ctx->prof_timing) {
+        a = take_event(ctx);
+        b = take_event(ctx);
+    }
+    if (a && b) cudaEventRecord(a, ctx->stream);
+    launch_level_kernel(k, v, grid, arg, ctx->stream);
+    if (a && b) {
+        cudaEventRecord(b, ctx->stream);
+        ctx->recs.push_back({(int)k, a, b});
+    }
+}
+
+// Folds finished event pairs into the per-kernel totals (stream must be idle).
+void collect_profile(orb_ctx *ctx) {
+    for (auto &r : ctx->recs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.kind] += ms;
+        ctx->ev_pool.push_back(r.a);
+        ctx->ev_pool.push_back(r.b);
+    }
+    ctx->recs.clear();
+    cudaGetLastError();
+}
+
+void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
+    const int g = pass_grid(ctx);
+    run_kernel(ctx, kKPartCount, v, g);
+    run_kernel(ctx, kKPartScan, v, g);
+    run_kernel(ctx, kKPartTables, v, g);
+    run_kernel(ctx, kKPartSwap, v, g);
+    run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
+}
+
 // Bisection of every cell of the level to completion (found or capped).
 orb_status run_bisection(orb_ctx *ctx, const Level &v, uint32_t *passes) {
     for (int pass = 0;; ++pass) {
         if (pass > 64) return fail(ctx, ORB_ERR_TIMEOUT, "bisection did not finish in 64 passes");
         ORB_CUDA(cudaMemsetAsync(&ctx->counters.p->any_active, 0, sizeof(uint32_t), ctx->stream));
-        launch_hist(v, pass_grid(ctx), ctx->stream);
-        launch_resolve(v, ctx->stream);
+        run_kernel(ctx, kKHist, v, pass_grid(ctx));
+        run_kernel(ctx, kKResolve, v, pass_grid(ctx));
         ORB_CUDA(cudaGetLastError());
         ORB_CUDA(cudaMemcpyAsync(&ctx->h_counters->any_active, &ctx->counters.p->any_active,
                                  sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -266,6 +328,8 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->tile_ge.release(); ctx->tile_le.release(); ctx->tile_ge_cnt.release(); ctx->tile_le_cnt.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    collect_profile(ctx);
+    for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -320,16 +384,17 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     }
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
+    ctx->launches[kKInit] += 1;
     launch_init(v, n, lower, upper, d, (int)heap_cells, s);
     ORB_CUDA(cudaGetLastError());
     uint32_t passes = 0;
     for (uint32_t l = 1; l <= levels; ++l) {
         v.base = (1 << (l - 1)) - 1;  // src/orbit.cpp:104-107
         v.C = 1 << (l - 1);
-        launch_plan(v, s);
+        run_kernel(ctx, kKPlan, v, 1);
         st = run_bisection(ctx, v, &passes);
         if (st != ORB_OK) return st;
-        launch_partition(v, pass_grid(ctx), true, s);
+        partition_level(ctx, v, true);
         ORB_CUDA(cudaGetLastError());
     }
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
@@ -353,6 +418,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     ORB_CUDA(cudaStreamSynchronize(s));
     float dev_ms = 0.f;
     ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
+    collect_profile(ctx);
+    for (int k = 0; k < kNumKernels; ++k) ctx->prof_bytes[k] += (double)ctx->h_counters->bytes[k];
     if (!dev) ORB_CUDA(cudaEventElapsedTime(&d2h_ms, ctx->ev[2], ctx->ev[3]));
     if (info) {
         std::memset(info, 0, sizeof *info);
@@ -388,6 +455,7 @@ orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float
         dy = ctx->y.p;
         dz = ctx->z.p;
     }
+    ctx->launches[kKGenerate] += 1;
     if (kind == ORB_GEN_UNIFORM) {
         launch_gen_uniform(seed, n, dx, dy, dz, ctx->stream);
     } else {
@@ -499,6 +567,27 @@ static orb_status service_prepare(orb_ctx *ctx, const orb_cell_t *cells, uint32_
         ids[i] = (int)id;
     }
     cudaStream_t s = ctx->stream;
+    // Size the per-tile buffers from the cells' actual ranges; reject overlapping cells
+    // (each tile and each rank table entry must belong to exactly one cell).
+    std::vector<uint2> rg(ctx->loaded_cells);
+    ORB_CUDA(cudaMemcpyAsync(rg.data(), ctx->ranges.p, rg.size() * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    ORB_CUDA(cudaStreamSynchronize(s));
+    std::vector<std::pair<uint32_t, uint32_t>> spans;
+    uint64_t tiles = 0;
+    for (uint32_t i = 0; i < n_cells; ++i) {
+        const uint2 r = rg[ids[i]];
+        if (r.y < r.x || r.y > ctx->loaded_n) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "corrupt range map");
+        tiles += (r.y - r.x + kTile - 1) / kTile;
+        if (r.y > r.x) spans.emplace_back(r.x, r.y);
+    }
+    std::sort(spans.begin(), spans.end());
+    for (size_t i = 1; i < spans.size(); ++i)
+        if (spans[i].first < spans[i - 1].second)
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "cells with overlapping particle ranges");
+    ORB_CUDA(ctx->tile_ge.ensure(tiles + 2));
+    ORB_CUDA(ctx->tile_le.ensure(tiles + 2));
+    ORB_CUDA(ctx->tile_ge_cnt.ensure(tiles + 2));
+    ORB_CUDA(ctx->tile_le_cnt.ensure(tiles + 2));
     // Each cell is placed at heap slot == id, so child slots are 2id+1 and 2id+2.
     if (n_cells) {
         ORB_CUDA(cudaMemcpyAsync(ctx->slots.p, ids.data(), n_cells * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -541,10 +630,11 @@ orb_status orb_count_left(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cell
     if (st != ORB_OK || n_cells == 0) return st;
     cudaStream_t s = ctx->stream;
     ORB_CUDA(cudaMemsetAsync(ctx->out_counts.p, 0, n_cells * sizeof(uint32_t), s));
-    launch_plan(v, s);
-    launch_count_left(v, pass_grid(ctx), s);
+    run_kernel(ctx, kKPlan, v, 1);
+    run_kernel(ctx, kKCountLeft, v, pass_grid(ctx));
     ORB_CUDA(cudaGetLastError());
     std::vector<uint32_t> res(n_cells);
+    collect_profile(ctx);
     ORB_CUDA(cudaMemcpyAsync(res.data(), ctx->out_counts.p, n_cells * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     ORB_CUDA(cudaStreamSynchronize(s));
     for (uint32_t i = 0; i < n_cells; ++i)
@@ -560,10 +650,11 @@ orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells
     orb_status st = service_prepare(ctx, cells, n_cells, true, &v);
     if (st != ORB_OK || n_cells == 0) return st;
     cudaStream_t s = ctx->stream;
-    launch_plan(v, s);
-    launch_partition(v, pass_grid(ctx), false, s);
+    run_kernel(ctx, kKPlan, v, 1);
+    partition_level(ctx, v, false);
     ORB_CUDA(cudaGetLastError());
     ORB_CUDA(cudaStreamSynchronize(s));
+    collect_profile(ctx);
     return ORB_OK;
 }
 
@@ -590,6 +681,41 @@ orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells
     ORB_CUDA(cudaMemcpyAsync(ctx->ranges.p, ranges, n_cells * sizeof(uint2), cudaMemcpyHostToDevice, ctx->stream));
     ORB_CUDA(cudaStreamSynchronize(ctx->stream));
     return ORB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Profiling
+// ---------------------------------------------------------------------------------------
+orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    collect_profile(ctx);
+    for (int k = 0; k < kNumKernels; ++k) {
+        ctx->launches[k] = 0;
+        ctx->prof_ms[k] = 0.0;
+        ctx->prof_bytes[k] = 0.0;
+    }
+    ctx->prof_timing = enable_timing != 0;
+    return ORB_OK;
+}
+
+int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries) {
+    if (!ctx) return -1;
+    int n = 0;
+    for (int k = 0; k < kNumKernels; ++k) {
+        if (!ctx->launches[k]) continue;
+        if (out && n < max_entries) {
+            orb_kernel_stat &o = out[n];
+            std::memset(&o, 0, sizeof o);
+            std::strncpy(o.name, kKernelNames[k], sizeof(o.name) - 1);
+            o.launches = ctx->launches[k];
+            o.total_ms = ctx->prof_ms[k];
+            o.bytes = ctx->prof_bytes[k];
+        }
+        ++n;
+    }
+    return n;
 }
 
 }  // extern "C"

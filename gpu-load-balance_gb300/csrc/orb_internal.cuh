@@ -18,6 +18,23 @@ constexpr int kThreads = 256;
 
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2 };
 
+// Kernel kinds, for launch counting, event timing and algorithmic-byte accounting.
+enum Kernel : int {
+    kKInit = 0,
+    kKPlan,
+    kKHist,
+    kKResolve,
+    kKPartCount,
+    kKPartScan,
+    kKPartTables,
+    kKPartSwap,
+    kKPartFinish,
+    kKCountLeft,
+    kKGenerate,
+    kNumKernels
+};
+extern const char *const kKernelNames[kNumKernels];
+
 // Device-side counters of one build (read back at the end).
 struct BuildCounters {
     uint32_t degenerate;
@@ -26,6 +43,7 @@ struct BuildCounters {
     uint32_t max_iters;
     uint32_t any_active;  // set by the resolve step when a cell still needs a pass
     uint32_t pad[3];
+    unsigned long long bytes[16];  // algorithmic bytes per Kernel kind
 };
 
 // Everything a level's kernels need. Cells of the level are heap slots [base, base + C)
@@ -85,14 +103,10 @@ __device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {
     return axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
 }
 
-// Host-side launchers (orb_kernels.cu).
+// Host-side launchers (orb_kernels.cu). `grid` is the CTA count of the tile loops.
 void launch_init(const Level &v, uint64_t n, const float lower[3], const float upper[3],
                  uint32_t d, int heap_cells, cudaStream_t st);
-void launch_plan(const Level &v, cudaStream_t st);
-void launch_hist(const Level &v, int grid, cudaStream_t st);
-void launch_resolve(const Level &v, cudaStream_t st);
-void launch_partition(const Level &v, int grid, bool do_split, cudaStream_t st);
-void launch_count_left(const Level &v, int grid, cudaStream_t st);
+void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st);
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);
 void launch_gen_plummer(uint64_t seed, uint64_t n, const float *centres, const double *scales,

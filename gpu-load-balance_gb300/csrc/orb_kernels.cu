@@ -20,7 +20,16 @@
 #include "orb_internal.cuh"
 
 namespace orb {
+
+const char *const kKernelNames[kNumKernels] = {
+    "init", "plan", "count_left_hist", "bisect_resolve", "part_count", "part_scan",
+    "part_tables", "part_swap", "part_finish", "count_left", "generate"};
+
 namespace {
+
+__device__ __forceinline__ void add_bytes(const Level &v, Kernel k, unsigned long long b) {
+    atomicAdd(&v.counters->bytes[k], b);
+}
 
 // ------------------------------------------------------------------------------------
 // Block helpers
@@ -288,7 +297,10 @@ __global__ void __launch_bounds__(kThreads) k_hist(Level v) {
             }
         });
         below = block_sum(below, s_red);
-        if (threadIdx.x == 0 && below) atomicAdd(&v.below[tr.c], below);
+        if (threadIdx.x == 0) {
+            if (below) atomicAdd(&v.below[tr.c], below);
+            add_bytes(v, kKHist, 4ull * (tr.e1 - tr.e0));
+        }
         uint32_t *g = v.hist + v.hist_off[tr.c];
         for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
             const uint32_t h = s_hist[b];
@@ -347,6 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
     if (lane == 0) {
+        add_bytes(v, kKResolve, 8ull << K);  // bins read and cleared
         cell.cutMarginLeft = L;
         cell.cutMarginRight = R;
         cell.foundCut = st == kFound ? 1 : 0;
@@ -385,6 +398,7 @@ __global__ void __launch_bounds__(kThreads) k_part_count(Level v) {
         if (threadIdx.x == 0) {
             v.tile_ge_cnt[t] = ge;
             v.tile_le_cnt[t] = le;
+            add_bytes(v, kKPartCount, 4ull * (tr.e1 - tr.e0) + 8ull);
         }
     }
 }
@@ -458,6 +472,7 @@ __global__ void __launch_bounds__(kThreads) k_part_scan(Level v) {
             s = block_max(best, sh);
         }
         if (threadIdx.x == 0) {
+            add_bytes(v, kKPartScan, 16ull * nt + (nt ? 4ull * min((uint32_t)kTile, v.ranges[slot].y - v.ranges[slot].x) : 0ull));
             v.part_s[c] = s;
             v.part_ge[c] = ge_tot;
             v.part_le[c] = le_tot;
@@ -497,18 +512,27 @@ __global__ void __launch_bounds__(kThreads) k_part_tables(Level v) {
         uint32_t rk = fpre + p.x;   // 0-based left rank of the next key >= cut
         uint32_t lseen = lpre + p.y;  // keys <= cut before the current position
         const uint32_t pos0 = tr.e0 - rg.x;
+        uint32_t written = 0;
         for (uint32_t i = s0; i < s1; ++i) {
             const float k = s_keys[i];
             if (!(k < cut)) {
-                if (rk <= s) v.tl[rg.x + rk] = pos0 + i;
+                if (rk <= s) {
+                    v.tl[rg.x + rk] = pos0 + i;
+                    ++written;
+                }
                 ++rk;
             }
             if (!(k > cut)) {
                 const uint32_t rr = le_tot - lseen - 1;  // 0-based right rank
-                if (rr < s) v.tr[rg.x + rr] = pos0 + i;
+                if (rr < s) {
+                    v.tr[rg.x + rr] = pos0 + i;
+                    ++written;
+                }
                 ++lseen;
             }
         }
+        written = block_sum(written, sh);
+        if (threadIdx.x == 0) add_bytes(v, kKPartTables, 4ull * m + 4ull * written);
         __syncthreads();
     }
 }
@@ -538,6 +562,8 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
         const uint32_t b = v.ranges[level_slot(v, c)].x;
         for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x)
             swap_particles(v, b + v.tl[b + k], b + v.tr[b + k]);
+        // per pair: 2 x 16 B read + 2 x 16 B written (x,y,z,idx) + 8 B of rank tables
+        if (threadIdx.x == 0) add_bytes(v, kKPartSwap, 72ull * (k1 - k0));
     }
 }
 
@@ -620,7 +646,10 @@ __global__ void __launch_bounds__(kThreads) k_count_left(Level v) {
         uint32_t cnt = 0;
         for_keys(axis_keys(v, eff_axis(cell.cutAxis)), tr.e0, tr.e1, [&](float k) { cnt += k < cut; });
         cnt = block_sum(cnt, s_red);
-        if (threadIdx.x == 0 && cnt) atomicAdd(&v.out_counts[tr.c], cnt);
+        if (threadIdx.x == 0) {
+            if (cnt) atomicAdd(&v.out_counts[tr.c], cnt);
+            add_bytes(v, kKCountLeft, 4ull * (tr.e1 - tr.e0));
+        }
     }
 }
 
@@ -723,26 +752,23 @@ void launch_init(const Level &v, uint64_t n, const float lower[3], const float u
                                                         heap_cells);
 }
 
-void launch_plan(const Level &v, cudaStream_t st) { k_plan<<<1, 1024, 0, st>>>(v); }
-
-void launch_hist(const Level &v, int grid, cudaStream_t st) {
-    k_hist<<<grid, kThreads, 0, st>>>(v);
-}
-
-void launch_resolve(const Level &v, cudaStream_t st) {
-    k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-}
-
-void launch_partition(const Level &v, int grid, bool do_split, cudaStream_t st) {
-    k_part_count<<<grid, kThreads, 0, st>>>(v);
-    k_part_scan<<<grid_for(v.C, 1, grid), kThreads, 0, st>>>(v);
-    k_part_tables<<<grid, kThreads, 0, st>>>(v);
-    k_part_swap<<<grid, kThreads, 0, st>>>(v);
-    k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, do_split ? 1 : 0);
-}
-
-void launch_count_left(const Level &v, int grid, cudaStream_t st) {
-    k_count_left<<<grid, kThreads, 0, st>>>(v);
+void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st) {
+    switch (k) {
+        case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
+        case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKResolve:
+            k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
+            break;
+        case kKPartCount: k_part_count<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartScan: k_part_scan<<<grid_for(v.C, 1, grid), kThreads, 0, st>>>(v); break;
+        case kKPartTables: k_part_tables<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartSwap: k_part_swap<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartFinish:
+            k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, arg);
+            break;
+        case kKCountLeft: k_count_left<<<grid, kThreads, 0, st>>>(v); break;
+        default: break;
+    }
 }
 
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,

@@ -62,6 +62,7 @@ EXPORTS = [
     "orb_abi_version", "orb_status_string", "orb_last_error", "orb_ctx_create",
     "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
     "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
+    "orb_profile_reset", "orb_profile_read",
 ]
 
 
@@ -131,6 +132,11 @@ class BuildInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64),
+                ("total_ms", ctypes.c_double), ("bytes", ctypes.c_double)]
+
+
 class Opts(ctypes.Structure):
     _fields_ = [("reserve_particles", ctypes.c_uint64), ("reserve_leaves", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32)]
@@ -178,6 +184,10 @@ def load(path: str = LIB_PATH):
         f.argtypes = [vp, vp, u32]
     L.orb_generate.restype = ctypes.c_int
     L.orb_generate.argtypes = [vp, ctypes.c_int, u64, u64, vp, vp, vp, u32]
+    L.orb_profile_reset.restype = ctypes.c_int
+    L.orb_profile_reset.argtypes = [vp, ctypes.c_int]
+    L.orb_profile_read.restype = ctypes.c_int
+    L.orb_profile_read.argtypes = [vp, ctypes.POINTER(KernelStat), ctypes.c_int]
     _lib = L
     return L
 
@@ -257,6 +267,19 @@ class Context:
         x, y, z = (np.empty(n, np.float32) for _ in range(3))
         self.generate(kind, seed, n, x, y, z)
         return x, y, z
+
+    # profiling -----------------------------------------------------------------------
+    def profile_reset(self, timing: bool = False):
+        self._check(self.lib.orb_profile_reset(self.h, 1 if timing else 0))
+
+    def profile(self) -> dict:
+        """{kernel name: {launches, total_ms, bytes}} since the last profile_reset."""
+        n = self.lib.orb_profile_read(self.h, None, 0)
+        arr = (KernelStat * max(n, 1))()
+        n = self.lib.orb_profile_read(self.h, arr, n)
+        return {arr[i].name.decode(): {"launches": int(arr[i].launches),
+                                       "total_ms": float(arr[i].total_ms),
+                                       "bytes": float(arr[i].bytes)} for i in range(n)}
 
     # service layer -------------------------------------------------------------------
     def load_particles(self, x, y, z, max_cells: int, device_pointers: bool = False):

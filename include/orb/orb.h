@@ -152,6 +152,23 @@ orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells
 orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float *x, float *y,
                         float *z, uint32_t flags);
 
+/*
+ * Per-kernel profile of a context (no reference counterpart; the reference prints phase
+ * wall-clock timers, src/orbit.cpp:284-286). Launch counts are always kept; with
+ * enable_timing, every launch is bracketed by CUDA events on the context stream and the
+ * durations are summed. `bytes` is the algorithmic traffic those launches moved (keys read,
+ * table entries written, particles swapped), counted on the device.
+ */
+typedef struct orb_kernel_stat {
+    char name[32];
+    uint64_t launches;
+    double total_ms;
+    double bytes;
+} orb_kernel_stat;
+orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing);
+/* Writes up to max_entries stats (kernels launched at least once); returns how many exist. */
+int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,8 @@ def assert_same(res, ref, gx, gy, gz):
     assert d is None, f"heap differs first at cell {d[0]}:\n gpu {d[1]}\n cpu {d[2]}"
     assert np.array_equal(res.ranges, ref.ranges[0]), "range map differs"
     assert np.array_equal(res.perm, ref.perm), "particle order differs"
-    assert np.array_equal(gx, ref.x) and np.array_equal(gy, ref.y) and np.array_equal(gz, ref.z)
+    for a, b in ((gx, ref.x), (gy, ref.y), (gz, ref.z)):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), "coordinates differ"
 
 
 def run_both(ctx, oracle, x, y, z, d, levels=0, **kw):
@@ -121,7 +122,7 @@ def test_device_pointers(ctx, oracle):
     assert res.heap.tobytes() == ref.heap.tobytes()
     assert np.array_equal(res.ranges, ref.ranges[0])
     assert np.array_equal(tp.cpu().numpy().view(np.uint32), ref.perm)
-    assert np.array_equal(tx.cpu().numpy(), ref.x)
+    assert np.array_equal(tx.cpu().numpy().view(np.uint32), ref.x.view(np.uint32))
 
 
 def test_service_layer(ctx, engine, oracle):
@@ -172,7 +173,7 @@ def test_service_layer(ctx, engine, oracle):
     assert heap.tobytes() == ref.heap.tobytes()
     assert np.array_equal(ctx.get_ranges(heap_cells), ref.ranges[0])
     sx, sy, sz, sp = ctx.store_particles()
-    assert np.array_equal(sp, ref.perm) and np.array_equal(sx, ref.x)
+    assert np.array_equal(sp, ref.perm) and np.array_equal(sx.view(np.uint32), ref.x.view(np.uint32))
 
 
 def test_large_parity(ctx, oracle):
