@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liborb_gb300.so")
-SOURCES = ["orb_kernels.cu", "orb_api.cu"]
+SOURCES = ["orb_kernels.cu", "orb_api.cu", "orb_static.cu"]
 HEADERS = ["orb_internal.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -62,8 +62,10 @@ EXPORTS = [
     "orb_abi_version", "orb_status_string", "orb_last_error", "orb_ctx_create",
     "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
     "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
-    "orb_profile_reset", "orb_profile_read",
+    "orb_profile_reset", "orb_profile_read", "orb_count_left_static",
 ]
+
+ORB_STATIC_MAX_CELLS = 65536
 
 
 class OrbError(RuntimeError):
@@ -188,6 +190,8 @@ def load(path: str = LIB_PATH):
     L.orb_profile_reset.argtypes = [vp, ctypes.c_int]
     L.orb_profile_read.restype = ctypes.c_int
     L.orb_profile_read.argtypes = [vp, ctypes.POINTER(KernelStat), ctypes.c_int]
+    L.orb_count_left_static.restype = ctypes.c_int
+    L.orb_count_left_static.argtypes = [vp, vp, vp, u64, vp, u32, vp, u32, vp, vp]
     _lib = L
     return L
 
@@ -200,6 +204,17 @@ def _ptr(a):
     if hasattr(a, "data_ptr"):  # torch tensor
         return a.data_ptr()
     return int(a)
+
+
+def count_left_static(x, y, z, n: int, cells, n_cells: int, ranges, n_ranges: int, out,
+                      stream=None):
+    """orb_count_left_static: every argument is device memory (tensors or pointers); the
+    call enqueues on `stream` (a raw cudaStream_t value, None = default stream)."""
+    lib = load()
+    st = lib.orb_count_left_static(_ptr(x), _ptr(y), _ptr(z), n, _ptr(cells), n_cells,
+                                   _ptr(ranges), n_ranges, _ptr(out), stream)
+    if st != 0:
+        raise OrbError(st, "orb_count_left_static")
 
 
 @dataclass

@@ -169,6 +169,31 @@ orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing);
 /* Writes up to max_entries stats (kernels launched at least once); returns how many exist. */
 int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries);
 
+/*
+ * Count-left that allocates nothing. It has no counterpart in the reference; it is the
+ * service count-left (same `key < getCut()` rule on cutAxis, found cells left untouched)
+ * for callers that must not allocate device memory while they run. Examples are a
+ * simulation code that has reserved the whole device in its own memory pool, where
+ * cudaMalloc would fail or fragment that pool, or one that cannot take the device-wide
+ * synchronisation cudaMalloc/cudaFree imply while its other streams are busy.
+ *   x, y, z   n device coordinates;  cells: n_cells device orb_cell_t
+ *   ranges    device range map, 2 uint32 {begin,end} per cell id, n_ranges ids; a cell
+ *             whose id or range lies outside the map or [0,n] counts as empty
+ *   out       device uint32[n_cells]
+ *   stream    cudaStream_t to run on (NULL = default stream); the call only enqueues work
+ * Scratch is one static device array of ORB_STATIC_MAX_CELLS cells (512 KiB per GPU,
+ * held until the process exits); n_cells above that returns ORB_ERR_CAPACITY. The call
+ * uses the calling thread's current device. Its first call on a device resolves the
+ * array's address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the one array (the kernels clear it first), so calls that overlap on
+ * the GPU, on different streams or threads, race and must be serialised by the caller.
+ */
+#define ORB_STATIC_MAX_CELLS 65536
+orb_status orb_count_left_static(const float *x, const float *y, const float *z, uint64_t n,
+                                 const orb_cell_t *cells, uint32_t n_cells,
+                                 const uint32_t *ranges, uint32_t n_ranges, uint32_t *out,
+                                 void *stream);
+
 #ifdef __cplusplus
 }
 #endif
