@@ -64,13 +64,13 @@ struct orb_ctx {
     std::string err;
 
     DevBuf<float> x, y, z;
-    DevBuf<uint32_t> idx, tl, tr;
+    DevBuf<uint32_t> idx;
     DevBuf<orb_cell_t> heap;
     DevBuf<uint2> ranges;
-    DevBuf<uint32_t> tile_off, hist_off, below, part_s, part_ge, part_le, out_counts;
+    DevBuf<uint32_t> tile_off, hist_off, below, part_s, part_i, part_le, out_counts;
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
-    DevBuf<uint32_t> tile_ge, tile_le, tile_ge_cnt, tile_le_cnt;
+    DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
     DevBuf<int> slots;
     DevBuf<BuildCounters> counters;
     DevBuf<orb_cell_t> staging;
@@ -121,19 +121,27 @@ bool is_device_ptr(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Level buffers for up to `max_cells` cells per level and `max_tiles` tiles.
+orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
+    ORB_CUDA(ctx->ge_bits.ensure(ptiles * kPWords));
+    ORB_CUDA(ctx->le_bits.ensure(ptiles * kPWords));
+    ORB_CUDA(ctx->pt_ge.ensure(ptiles));
+    ORB_CUDA(ctx->pt_le.ensure(ptiles));
+    ORB_CUDA(ctx->pt_ge_pre.ensure(ptiles + 1));
+    ORB_CUDA(ctx->pt_le_pre.ensure(ptiles + 1));
+    return ORB_OK;
+}
+
+// Level buffers for up to `max_cells` cells per level over n particles.
 orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, uint32_t heap_cells) {
-    const uint64_t max_tiles = n / kTile + max_cells + 2;
+    const uint64_t max_ptiles = n / kPTile + max_cells + 2;
     const uint64_t max_bins = n / 2 + 16ull * max_cells + 16;
-    ORB_CUDA(ctx->tl.ensure(n + 1));
-    ORB_CUDA(ctx->tr.ensure(n + 1));
     ORB_CUDA(ctx->heap.ensure(heap_cells));
     ORB_CUDA(ctx->ranges.ensure(heap_cells));
     ORB_CUDA(ctx->tile_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->hist_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->below.ensure(max_cells));
     ORB_CUDA(ctx->part_s.ensure(max_cells));
-    ORB_CUDA(ctx->part_ge.ensure(max_cells));
+    ORB_CUDA(ctx->part_i.ensure(max_cells));
     ORB_CUDA(ctx->part_le.ensure(max_cells));
     ORB_CUDA(ctx->out_counts.ensure(max_cells));
     ORB_CUDA(ctx->hist_k.ensure(max_cells));
@@ -141,12 +149,9 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->iters.ensure(max_cells));
     ORB_CUDA(ctx->slots.ensure(max_cells));
     ORB_CUDA(ctx->hist.ensure(max_bins, true));
-    ORB_CUDA(ctx->tile_ge.ensure(max_tiles));
-    ORB_CUDA(ctx->tile_le.ensure(max_tiles));
-    ORB_CUDA(ctx->tile_ge_cnt.ensure(max_tiles));
-    ORB_CUDA(ctx->tile_le_cnt.ensure(max_tiles));
+    ORB_CUDA(ctx->ptile_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->counters.ensure(1, true));
-    return ORB_OK;
+    return ensure_ptile_buffers(ctx, max_ptiles);
 }
 
 Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
@@ -166,15 +171,16 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.iters = ctx->iters.p;
     v.hist = ctx->hist.p;
     v.below = ctx->below.p;
-    v.tile_ge = ctx->tile_ge.p;
-    v.tile_le = ctx->tile_le.p;
-    v.tile_ge_cnt = ctx->tile_ge_cnt.p;
-    v.tile_le_cnt = ctx->tile_le_cnt.p;
+    v.ptile_off = ctx->ptile_off.p;
+    v.ge_bits = ctx->ge_bits.p;
+    v.le_bits = ctx->le_bits.p;
+    v.pt_ge = ctx->pt_ge.p;
+    v.pt_le = ctx->pt_le.p;
+    v.pt_ge_pre = ctx->pt_ge_pre.p;
+    v.pt_le_pre = ctx->pt_le_pre.p;
     v.part_s = ctx->part_s.p;
-    v.part_ge = ctx->part_ge.p;
+    v.part_i = ctx->part_i.p;
     v.part_le = ctx->part_le.p;
-    v.tl = ctx->tl.p;
-    v.tr = ctx->tr.p;
     v.out_counts = ctx->out_counts.p;
     v.counters = ctx->counters.p;
     return v;
@@ -223,9 +229,9 @@ void collect_profile(orb_ctx *ctx) {
 
 void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     const int g = pass_grid(ctx);
-    run_kernel(ctx, kKPartCount, v, g);
-    run_kernel(ctx, kKPartScan, v, g);
-    run_kernel(ctx, kKPartTables, v, g);
+    run_kernel(ctx, kKPartClassify, v, g);
+    run_kernel(ctx, kKPartScan, v, 1);
+    run_kernel(ctx, kKPartCells, v, g);
     run_kernel(ctx, kKPartSwap, v, g);
     run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
 }
@@ -320,12 +326,13 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->x.release(); ctx->y.release(); ctx->z.release();
-    ctx->idx.release(); ctx->tl.release(); ctx->tr.release();
+    ctx->idx.release();
     ctx->heap.release(); ctx->ranges.release();
     ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release();
-    ctx->part_s.release(); ctx->part_ge.release(); ctx->part_le.release(); ctx->out_counts.release();
+    ctx->part_s.release(); ctx->part_i.release(); ctx->part_le.release(); ctx->out_counts.release();
     ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
-    ctx->tile_ge.release(); ctx->tile_le.release(); ctx->tile_ge_cnt.release(); ctx->tile_le_cnt.release();
+    ctx->ptile_off.release(); ctx->ge_bits.release(); ctx->le_bits.release(); ctx->pt_ge.release();
+    ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
@@ -577,17 +584,17 @@ static orb_status service_prepare(orb_ctx *ctx, const orb_cell_t *cells, uint32_
     for (uint32_t i = 0; i < n_cells; ++i) {
         const uint2 r = rg[ids[i]];
         if (r.y < r.x || r.y > ctx->loaded_n) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "corrupt range map");
-        tiles += (r.y - r.x + kTile - 1) / kTile;
+        tiles += (r.y - r.x + kPTile - 1) / kPTile;
         if (r.y > r.x) spans.emplace_back(r.x, r.y);
     }
     std::sort(spans.begin(), spans.end());
     for (size_t i = 1; i < spans.size(); ++i)
         if (spans[i].first < spans[i - 1].second)
             return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "cells with overlapping particle ranges");
-    ORB_CUDA(ctx->tile_ge.ensure(tiles + 2));
-    ORB_CUDA(ctx->tile_le.ensure(tiles + 2));
-    ORB_CUDA(ctx->tile_ge_cnt.ensure(tiles + 2));
-    ORB_CUDA(ctx->tile_le_cnt.ensure(tiles + 2));
+    {
+        orb_status pst = ensure_ptile_buffers(ctx, tiles + 2);
+        if (pst != ORB_OK) return pst;
+    }
     // Each cell is placed at heap slot == id, so child slots are 2id+1 and 2id+2.
     if (n_cells) {
         ORB_CUDA(cudaMemcpyAsync(ctx->slots.p, ids.data(), n_cells * sizeof(int), cudaMemcpyHostToDevice, s));

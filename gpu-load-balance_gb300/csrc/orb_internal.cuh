@@ -12,7 +12,9 @@ namespace orb {
 static_assert(sizeof(orb_cell_t) == 52, "orb_cell_t must keep the reference's 52-byte Cell layout");
 
 constexpr int kMaxIterations = 32;   // bisection cap, src/orbit.cpp:149
-constexpr int kTile = 8192;          // keys per tile of the multi-CTA passes
+constexpr int kTile = 8192;          // keys per tile of the count-left passes
+constexpr int kPTile = 4096;         // positions per tile of the partition passes
+constexpr int kPWords = kPTile / 32; // bitmask words per partition tile
 constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
 constexpr int kThreads = 256;
 
@@ -24,9 +26,9 @@ enum Kernel : int {
     kKPlan,
     kKHist,
     kKResolve,
-    kKPartCount,
+    kKPartClassify,
     kKPartScan,
-    kKPartTables,
+    kKPartCells,
     kKPartSwap,
     kKPartFinish,
     kKCountLeft,
@@ -65,15 +67,16 @@ struct Level {
     uint32_t *hist;         // histogram pool (kept all-zero between passes)
     uint32_t *below;        // [C]   keys below the left margin in the current pass
     // partition
-    uint32_t *tile_ge;      // [tiles] keys >= cut per tile, then exclusive prefix in-cell
-    uint32_t *tile_le;      // [tiles] keys <= cut per tile, then exclusive prefix in-cell
-    uint32_t *tile_ge_cnt;  // [tiles] raw counts kept for the table pass
-    uint32_t *tile_le_cnt;
+    uint32_t *ptile_off;    // [C+1] first partition tile of each cell
+    uint32_t *ge_bits;      // [ptiles * kPWords] bit p: key >= cut
+    uint32_t *le_bits;      // [ptiles * kPWords] bit p: key <= cut
+    uint32_t *pt_ge;        // [ptiles] set bits per tile
+    uint32_t *pt_le;
+    uint32_t *pt_ge_pre;    // [ptiles+1] exclusive prefix over all tiles of the level
+    uint32_t *pt_le_pre;
     uint32_t *part_s;       // [C] number of Hoare swaps
-    uint32_t *part_ge;      // [C] keys >= cut in the cell
+    uint32_t *part_i;       // [C] split index (cell-relative); n when clamped
     uint32_t *part_le;      // [C] keys <= cut in the cell
-    uint32_t *tl;           // [N] positions of keys >= cut from the left (by rank)
-    uint32_t *tr;           // [N] positions of keys <= cut from the right (by rank)
     uint32_t *out_counts;   // service calls: per-cell result
     BuildCounters *counters;
 };

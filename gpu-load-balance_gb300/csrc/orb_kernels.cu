@@ -22,8 +22,8 @@
 namespace orb {
 
 const char *const kKernelNames[kNumKernels] = {
-    "init", "plan", "count_left_hist", "bisect_resolve", "part_count", "part_scan",
-    "part_tables", "part_swap", "part_finish", "count_left", "generate"};
+    "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
+    "part_cells", "part_swap", "part_finish", "count_left", "generate"};
 
 namespace {
 
@@ -234,21 +234,25 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
     const int C = v.C, tid = threadIdx.x, nt = blockDim.x;
     const int per = (C + nt - 1) / nt;
     const int c0 = min(C, tid * per), c1 = min(C, c0 + per);
-    uint32_t ta = 0, tb = 0;
+    uint32_t ta = 0, tb = 0, tp = 0;
     for (int c = c0; c < c1; ++c) {
         const uint2 rg = v.ranges[level_slot(v, c)];
         const uint32_t n = rg.y - rg.x;
         ta += (n + kTile - 1) / kTile;
         tb += 1u << tree_depth(n);
+        tp += (n + kPTile - 1) / kPTile;
     }
-    uint32_t tot_a, tot_b;
+    uint32_t tot_a, tot_b, tot_p, unused;
     uint2 p = block_excl_scan2(ta, tb, sh, &tot_a, &tot_b);
+    uint32_t pp = block_excl_scan2(tp, 0u, sh, &tot_p, &unused).x;
     for (int c = c0; c < c1; ++c) {
         const uint2 rg = v.ranges[level_slot(v, c)];
         const uint32_t n = rg.y - rg.x;
         const int k = tree_depth(n);
         v.tile_off[c] = p.x;
         v.hist_off[c] = p.y;
+        v.ptile_off[c] = pp;
+        pp += (n + kPTile - 1) / kPTile;
         v.hist_k[c] = (uint8_t)k;
         v.state[c] = kActive;
         v.iters[c] = 0;
@@ -259,6 +263,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
     if (tid == 0) {
         v.tile_off[C] = tot_a;
         v.hist_off[C] = tot_b;
+        v.ptile_off[C] = tot_p;
     }
 }
 
@@ -374,196 +379,306 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
 
 // ------------------------------------------------------------------------------------
 // Partition
+//
+// Partition tiles are kPTile consecutive positions of one cell. Per tile, the classify
+// pass stores two bitmasks (key >= cut, key <= cut) and their counts; one scan over all
+// tiles of the level gives every tile its exclusive prefix (in-cell prefix = difference
+// with the cell's first tile). A warp per cell then finds s and the split index i, and a
+// CTA per tile performs the swaps of the pairs whose left element lies in that tile.
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ float cell_cut(const orb_cell_t &c) {
     return mid_cut(c.cutMarginLeft, c.cutMarginRight);
 }
 
-// P1: keys >= cut and keys <= cut per tile.
-__global__ void __launch_bounds__(kThreads) k_part_count(Level v) {
-    __shared__ uint32_t s_red[32];
-    const uint32_t total = v.tile_off[v.C];
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) {
+    const int lane = threadIdx.x & 31;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    *total = __shfl_sync(0xffffffffu, inc, 31);
+    return inc - v;
+}
+
+// P1: bitmasks and counts of keys >= cut and keys <= cut per partition tile.
+__global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
+    __shared__ uint32_t s_cnt[2][kThreads / 32];
+    const uint32_t total = v.ptile_off[v.C];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const TileRef tr = tile_ref(v, t);
-        const orb_cell_t &cell = v.heap[tr.slot];
+        const int c = find_cell(v.ptile_off, v.C, t);
+        const int slot = level_slot(v, c);
+        const orb_cell_t &cell = v.heap[slot];
         const float cut = cell_cut(cell);
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
-        uint32_t ge = 0, le = 0;
-        for_keys(keys, tr.e0, tr.e1, [&](float k) {
-            ge += !(k < cut);
-            le += !(k > cut);
-        });
-        ge = block_sum(ge, s_red);
-        le = block_sum(le, s_red);
-        if (threadIdx.x == 0) {
-            v.tile_ge_cnt[t] = ge;
-            v.tile_le_cnt[t] = le;
-            add_bytes(v, kKPartCount, 4ull * (tr.e1 - tr.e0) + 8ull);
-        }
-    }
-}
-
-constexpr int kSeg = kTile / kThreads;  // consecutive keys per thread in the ordered passes
-
-// Loads one tile's keys into shared memory (coalesced) for an in-order walk.
-__device__ __forceinline__ void load_tile(const float *keys, uint32_t e0, uint32_t e1, float *s_keys) {
-    for (uint32_t i = threadIdx.x; i < e1 - e0; i += blockDim.x) s_keys[i] = __ldg(keys + e0 + i);
-    __syncthreads();
-}
-
-// P1.5: per cell, prefix sums over its tiles and the swap count s.
-__global__ void __launch_bounds__(kThreads) k_part_scan(Level v) {
-    __shared__ uint32_t sh[96];
-    __shared__ float s_keys[kTile];
-    for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
-        const int slot = level_slot(v, c);
-        const uint32_t t0 = v.tile_off[c], nt = v.tile_off[c + 1] - t0;
+        const uint2 rg = v.ranges[slot];
+        const uint32_t p0 = rg.x + (t - v.ptile_off[c]) * (uint32_t)kPTile;
+        const uint32_t m = min((uint32_t)kPTile, rg.y - p0);
+        uint32_t *gw = v.ge_bits + (size_t)t * kPWords;
+        uint32_t *lw = v.le_bits + (size_t)t * kPWords;
         uint32_t cg = 0, cl = 0;
-        for (uint32_t b = 0; b < nt; b += blockDim.x) {
-            const uint32_t i = b + threadIdx.x;
-            const uint32_t a = i < nt ? v.tile_ge_cnt[t0 + i] : 0u;
-            const uint32_t l = i < nt ? v.tile_le_cnt[t0 + i] : 0u;
-            uint32_t ta, tl;
-            const uint2 p = block_excl_scan2(a, l, sh, &ta, &tl);
-            if (i < nt) {
-                v.tile_ge[t0 + i] = cg + p.x;
-                v.tile_le[t0 + i] = cl + p.y;
-            }
-            cg += ta;
-            cl += tl;
+        constexpr int kWordsPerWarp = kPWords / (kThreads / 32);
+        float k[kWordsPerWarp];
+#pragma unroll
+        for (int j = 0; j < kWordsPerWarp; ++j) {
+            const uint32_t i = (uint32_t)(warp * kWordsPerWarp + j) * 32u + lane;
+            k[j] = i < m ? __ldg(keys + p0 + i) : 0.0f;
         }
-        const uint32_t ge_tot = cg, le_tot = cl;
-        __syncthreads();  // prefixes visible to the whole block
-        // First tile whose end boundary has f >= g (exists: f(n) >= 0 = g(n)).
-        uint32_t cross = 0xffffffffu;
-        for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
-            const uint32_t f_end = v.tile_ge[t0 + i] + v.tile_ge_cnt[t0 + i];
-            const uint32_t g_end = le_tot - (v.tile_le[t0 + i] + v.tile_le_cnt[t0 + i]);
-            if (f_end >= g_end) cross = min(cross, i);
-        }
-        cross = block_min(cross, sh);
-        uint32_t s = 0;
-        if (nt > 0) {
-            const uint32_t t = t0 + cross;
-            const uint2 rg = v.ranges[slot];
-            const uint32_t e0 = rg.x + cross * (uint32_t)kTile, e1 = min(rg.y, e0 + (uint32_t)kTile);
-            const orb_cell_t &cell = v.heap[slot];
-            const float cut = cell_cut(cell);
-            load_tile(axis_keys(v, eff_axis(cell.cutAxis)), e0, e1, s_keys);
-            const uint32_t m = e1 - e0;
-            const uint32_t s0 = min(m, threadIdx.x * (uint32_t)kSeg), s1 = min(m, s0 + kSeg);
-            uint32_t lg = 0, ll = 0;
-            for (uint32_t i = s0; i < s1; ++i) {
-                const float k = s_keys[i];
-                lg += !(k < cut);
-                ll += !(k > cut);
+#pragma unroll
+        for (int j = 0; j < kWordsPerWarp; ++j) {
+            const int w = warp * kWordsPerWarp + j;
+            const bool valid = (uint32_t)w * 32u + lane < m;
+            const uint32_t gb = __ballot_sync(0xffffffffu, valid && !(k[j] < cut));
+            const uint32_t lb = __ballot_sync(0xffffffffu, valid && !(k[j] > cut));
+            if (lane == 0) {
+                gw[w] = gb;
+                lw[w] = lb;
             }
-            uint32_t ta, tl;
-            const uint2 p = block_excl_scan2(lg, ll, sh, &ta, &tl);
-            uint32_t f = v.tile_ge[t] + p.x;
-            uint32_t gg = le_tot - v.tile_le[t] - p.y;
-            uint32_t best = min(f, gg);
-            for (uint32_t i = s0; i < s1; ++i) {
-                const float k = s_keys[i];
-                f += !(k < cut);
-                gg -= !(k > cut);
-                best = max(best, min(f, gg));
-            }
-            s = block_max(best, sh);
+            cg += __popc(gb);
+            cl += __popc(lb);
         }
+        if (lane == 0) {
+            s_cnt[0][warp] = cg;
+            s_cnt[1][warp] = cl;
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
-            add_bytes(v, kKPartScan, 16ull * nt + (nt ? 4ull * min((uint32_t)kTile, v.ranges[slot].y - v.ranges[slot].x) : 0ull));
-            v.part_s[c] = s;
-            v.part_ge[c] = ge_tot;
-            v.part_le[c] = le_tot;
+            uint32_t a = 0, b = 0;
+            for (int w = 0; w < kThreads / 32; ++w) {
+                a += s_cnt[0][w];
+                b += s_cnt[1][w];
+            }
+            v.pt_ge[t] = a;
+            v.pt_le[t] = b;
+            add_bytes(v, kKPartClassify, 4ull * m + 8ull * kPWords + 8ull);
         }
         __syncthreads();
     }
 }
 
-// P2: rank tables. tl[begin + k] = position of the (k+1)-th key >= cut for k <= s,
-// tr[begin + k] = position of the (k+1)-th key <= cut from the right for k < s.
-__global__ void __launch_bounds__(kThreads) k_part_tables(Level v) {
+// P2: exclusive prefix of the per-tile counts over every tile of the level (one CTA).
+// pt_ge_pre[t] = sum of pt_ge over tiles before t; entry [total] holds the grand total.
+__global__ void __launch_bounds__(1024) k_tile_scan(Level v) {
     __shared__ uint32_t sh[96];
-    __shared__ float s_keys[kTile];
-    const uint32_t total = v.tile_off[v.C];
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const TileRef tr = tile_ref(v, t);
-        const uint32_t s = v.part_s[tr.c], le_tot = v.part_le[tr.c];
-        const uint32_t fpre = v.tile_ge[t], lpre = v.tile_le[t];
-        const uint2 rg = v.ranges[tr.slot];
-        // Nothing of this tile can enter the tables: every rank here is beyond s.
-        const bool need_l = fpre <= s;
-        const bool need_r = (le_tot - lpre) > 0 && (le_tot - lpre - v.tile_le_cnt[t]) < s;
-        if (!need_l && !need_r) continue;
-        const orb_cell_t &cell = v.heap[tr.slot];
-        const float cut = cell_cut(cell);
-        load_tile(axis_keys(v, eff_axis(cell.cutAxis)), tr.e0, tr.e1, s_keys);
-        const uint32_t m = tr.e1 - tr.e0;
-        const uint32_t s0 = min(m, threadIdx.x * (uint32_t)kSeg), s1 = min(m, s0 + kSeg);
-        uint32_t lg = 0, ll = 0;
-        for (uint32_t i = s0; i < s1; ++i) {
-            const float k = s_keys[i];
-            lg += !(k < cut);
-            ll += !(k > cut);
-        }
-        uint32_t ta, tl;
-        const uint2 p = block_excl_scan2(lg, ll, sh, &ta, &tl);
-        uint32_t rk = fpre + p.x;   // 0-based left rank of the next key >= cut
-        uint32_t lseen = lpre + p.y;  // keys <= cut before the current position
-        const uint32_t pos0 = tr.e0 - rg.x;
-        uint32_t written = 0;
-        for (uint32_t i = s0; i < s1; ++i) {
-            const float k = s_keys[i];
-            if (!(k < cut)) {
-                if (rk <= s) {
-                    v.tl[rg.x + rk] = pos0 + i;
-                    ++written;
-                }
-                ++rk;
+    const uint32_t total = v.ptile_off[v.C];
+    const uint32_t per = (total + blockDim.x - 1) / blockDim.x;
+    const uint32_t a0 = min(total, threadIdx.x * per), a1 = min(total, a0 + per);
+    uint32_t sg = 0, sl = 0;
+    for (uint32_t t = a0; t < a1; ++t) {
+        sg += v.pt_ge[t];
+        sl += v.pt_le[t];
+    }
+    uint32_t tg, tl;
+    uint2 p = block_excl_scan2(sg, sl, sh, &tg, &tl);
+    for (uint32_t t = a0; t < a1; ++t) {
+        const uint32_t g = v.pt_ge[t], l = v.pt_le[t];
+        v.pt_ge_pre[t] = p.x;
+        v.pt_le_pre[t] = p.y;
+        p.x += g;
+        p.y += l;
+    }
+    if (threadIdx.x == 0) {
+        v.pt_ge_pre[total] = tg;
+        v.pt_le_pre[total] = tl;
+        add_bytes(v, kKPartScan, 16ull * total);
+    }
+}
+
+// Position (cell-relative) of the set bit with in-cell rank `rank` among the bitmasks of
+// tiles [t0, t1) (warp-cooperative; every lane returns the answer).
+__device__ uint32_t warp_select(const uint32_t *bits, const uint32_t *pre, uint32_t t0, uint32_t t1,
+                                uint32_t rank) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t base0 = pre[t0];
+    uint32_t lo = t0, hi = t1 - 1;  // largest t with pre[t] - base0 <= rank
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (pre[mid] - base0 <= rank)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const uint32_t r = rank - (pre[lo] - base0);
+    const uint32_t *w = bits + (size_t)lo * kPWords + lane * (kPWords / 32);
+    uint32_t words[kPWords / 32];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < kPWords / 32; ++j) {
+        words[j] = w[j];
+        cnt += __popc(words[j]);
+    }
+    uint32_t tot;
+    const uint32_t ex = warp_excl_scan(cnt, &tot);
+    const bool mine = r >= ex && r < ex + cnt;
+    uint32_t pos = 0;
+    if (mine) {
+        uint32_t rr = r - ex;
+#pragma unroll
+        for (int j = 0; j < kPWords / 32; ++j) {
+            const uint32_t pc = __popc(words[j]);
+            if (rr < pc) {
+                uint32_t word = words[j];
+                for (uint32_t q = 0; q < rr; ++q) word &= word - 1;  // drop rr lowest set bits
+                pos = (lo - t0) * (uint32_t)kPTile + (uint32_t)(lane * (kPWords / 32) + j) * 32u +
+                      (uint32_t)(__ffs(word) - 1);
+                rr = 0xffffffffu;
+                break;
             }
-            if (!(k > cut)) {
-                const uint32_t rr = le_tot - lseen - 1;  // 0-based right rank
-                if (rr < s) {
-                    v.tr[rg.x + rr] = pos0 + i;
-                    ++written;
-                }
-                ++lseen;
+            rr -= pc;
+        }
+    }
+    const uint32_t who = __ballot_sync(0xffffffffu, mine);
+    return __shfl_sync(0xffffffffu, pos, __ffs(who) - 1);
+}
+
+// P3: per cell (one warp): totals, the swap count s and the split index i.
+//   s = max_x min(f(x), g(x)), f(x) = #{>= cut in [0,x)}, g(x) = #{<= cut in [x,n)}
+//   i = min(L_{s+1}, R_s); i == n marks the clamped case (every key below the cut).
+__global__ void __launch_bounds__(kThreads) k_part_cells(Level v) {
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= v.C) return;
+    const int slot = level_slot(v, c);
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
+    const uint32_t G0 = v.pt_ge_pre[t0], L0 = v.pt_le_pre[t0];
+    const uint32_t ge_tot = v.pt_ge_pre[t1] - G0, le_tot = v.pt_le_pre[t1] - L0;
+    uint32_t s = 0, i = n;
+    if (t1 > t0) {
+        // crossing tile: first tile whose end has f >= g (the last tile always does)
+        uint32_t lo = t0, hi = t1 - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const uint32_t f_end = v.pt_ge_pre[mid + 1] - G0;
+            const uint32_t g_end = le_tot - (v.pt_le_pre[mid + 1] - L0);
+            if (f_end >= g_end)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        const uint32_t *gw = v.ge_bits + (size_t)lo * kPWords + lane * (kPWords / 32);
+        const uint32_t *lw = v.le_bits + (size_t)lo * kPWords + lane * (kPWords / 32);
+        uint32_t gwd[kPWords / 32], lwd[kPWords / 32];
+        uint32_t cg = 0, cl = 0;
+#pragma unroll
+        for (int j = 0; j < kPWords / 32; ++j) {
+            gwd[j] = gw[j];
+            lwd[j] = lw[j];
+            cg += __popc(gwd[j]);
+            cl += __popc(lwd[j]);
+        }
+        uint32_t tg, tl;
+        const uint32_t eg = warp_excl_scan(cg, &tg);
+        const uint32_t el = warp_excl_scan(cl, &tl);
+        uint32_t f = (v.pt_ge_pre[lo] - G0) + eg;
+        uint32_t g = le_tot - (v.pt_le_pre[lo] - L0) - el;
+        uint32_t best = min(f, g);
+#pragma unroll
+        for (int j = 0; j < kPWords / 32; ++j) {
+            uint32_t a = gwd[j], b = lwd[j];
+            for (int q = 0; q < 32; ++q) {
+                f += a & 1u;
+                g -= b & 1u;
+                a >>= 1;
+                b >>= 1;
+                best = max(best, min(f, g));
             }
         }
-        written = block_sum(written, sh);
-        if (threadIdx.x == 0) add_bytes(v, kKPartTables, 4ull * m + 4ull * written);
-        __syncthreads();
+        s = warp_max(best);
+        if (ge_tot > s) i = min(i, warp_select(v.ge_bits, v.pt_ge_pre, t0, t1, s));
+        if (s >= 1) i = min(i, warp_select(v.le_bits, v.pt_le_pre, t0, t1, le_tot - s));
+    }
+    if (lane == 0) {
+        v.part_s[c] = s;
+        v.part_i[c] = i;
+        v.part_le[c] = le_tot;
+        add_bytes(v, kKPartCells, 16ull * 3 + (t1 > t0 ? 3ull * 2 * 4 * kPWords : 0ull));
+    }
+}
+
+// Writes the cell-relative positions of the set bits of one tile's mask whose in-cell rank
+// lies in [lo, hi) to out[f(rank)], f(rank) = rank - lo (forward) or (top - rank) (reverse).
+// Block-cooperative; `sh` holds >= 96 words.
+__device__ __forceinline__ void emit_positions(const uint32_t *words, uint32_t rank_base,
+                                               uint32_t lo, uint32_t hi, uint32_t rel_base,
+                                               bool reverse, uint32_t top, uint32_t *out,
+                                               uint32_t *sh) {
+    const uint32_t tid = threadIdx.x;
+    const uint32_t w = tid < (uint32_t)kPWords ? words[tid] : 0u;
+    uint32_t ta, tb;
+    const uint2 ex = block_excl_scan2(__popc(w), 0u, sh, &ta, &tb);
+    uint32_t r = rank_base + ex.x;
+    uint32_t word = w;
+    while (word) {
+        const uint32_t b = (uint32_t)(__ffs(word) - 1);
+        word &= word - 1;
+        if (r >= lo && r < hi) out[reverse ? top - r : r - lo] = rel_base + tid * 32u + b;
+        ++r;
     }
 }
 
 __device__ __forceinline__ void swap_particles(const Level &v, uint32_t a, uint32_t b) {
-    float t;
-    t = v.x[a]; v.x[a] = v.x[b]; v.x[b] = t;
-    t = v.y[a]; v.y[a] = v.y[b]; v.y[b] = t;
-    t = v.z[a]; v.z[a] = v.z[b]; v.z[b] = t;
+    const float xa = v.x[a], xb = v.x[b];
+    const float ya = v.y[a], yb = v.y[b];
+    const float za = v.z[a], zb = v.z[b];
+    v.x[a] = xb;
+    v.x[b] = xa;
+    v.y[a] = yb;
+    v.y[b] = ya;
+    v.z[a] = zb;
+    v.z[b] = za;
     if (v.idx) {
-        uint32_t u = v.idx[a];
-        v.idx[a] = v.idx[b];
-        v.idx[b] = u;
+        const uint32_t ia = v.idx[a], ib = v.idx[b];
+        v.idx[a] = ib;
+        v.idx[b] = ia;
     }
 }
 
-// P3: the s Hoare swaps of every cell; tile j of a cell swaps pairs [j*kTile, (j+1)*kTile).
+// P4: the Hoare swaps. The CTA of tile t takes the pairs (L_k, R_k) whose left element
+// L_k lies in t (k < s); their right partners are the keys <= cut of left-to-right rank
+// le_tot-1-k, found in the right tiles' masks. Positions of each side are disjoint
+// (L_k < i <= R_k), so the CTAs never touch the same particle.
 __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
-    const uint32_t total = v.tile_off[v.C];
+    __shared__ uint32_t posL[kPTile];
+    __shared__ uint32_t posR[kPTile];
+    __shared__ uint32_t sh[96];
+    const uint32_t total = v.ptile_off[v.C];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const int c = find_cell(v.tile_off, v.C, t);
-        const uint32_t local = t - v.tile_off[c];
+        const int c = find_cell(v.ptile_off, v.C, t);
+        const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
         const uint32_t s = v.part_s[c];
-        const uint32_t k0 = local * (uint32_t)kTile;
-        if (k0 >= s) continue;
-        const uint32_t k1 = min(s, k0 + (uint32_t)kTile);
+        const uint32_t G0 = v.pt_ge_pre[t0];
+        const uint32_t ka = v.pt_ge_pre[t] - G0;
+        const uint32_t kb = min(s, v.pt_ge_pre[t + 1] - G0);
+        if (ka >= kb) continue;
+        const uint32_t cnt = kb - ka;
+        const uint32_t le_tot = v.part_le[c];
+        const uint32_t L0 = v.pt_le_pre[t0];
         const uint32_t b = v.ranges[level_slot(v, c)].x;
-        for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x)
-            swap_particles(v, b + v.tl[b + k], b + v.tr[b + k]);
-        // per pair: 2 x 16 B read + 2 x 16 B written (x,y,z,idx) + 8 B of rank tables
-        if (threadIdx.x == 0) add_bytes(v, kKPartSwap, 72ull * (k1 - k0));
+        // left elements: ranks [ka, kb) of this tile's >= mask, in order
+        emit_positions(v.ge_bits + (size_t)t * kPWords, ka, ka, kb, (t - t0) * (uint32_t)kPTile,
+                       false, 0u, posL, sh);
+        // right partners: left-to-right <= ranks [le_tot-kb, le_tot-ka); rank r pairs with
+        // k = le_tot-1-r, stored at posR[k - ka] = posR[(le_tot-1-ka) - r]
+        const uint32_t ra = le_tot - kb, rb = le_tot - ka;
+        uint32_t u0 = t0, uh = t1 - 1;  // largest u with in-cell prefix <= ra
+        while (u0 < uh) {
+            const uint32_t mid = (u0 + uh + 1) >> 1;
+            if (v.pt_le_pre[mid] - L0 <= ra)
+                u0 = mid;
+            else
+                uh = mid - 1;
+        }
+        for (uint32_t u = u0; u < t1 && v.pt_le_pre[u] - L0 < rb; ++u)
+            emit_positions(v.le_bits + (size_t)u * kPWords, v.pt_le_pre[u] - L0, ra, rb,
+                           (u - t0) * (uint32_t)kPTile, true, le_tot - 1 - ka, posR, sh);
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) swap_particles(v, b + posL[j], b + posR[j]);
+        if (threadIdx.x == 0) add_bytes(v, kKPartSwap, 64ull * cnt);
+        __syncthreads();
     }
 }
 
@@ -585,7 +700,7 @@ __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {
     c.cutMarginRight = c.upper[a];
 }
 
-// P4: split index, final swap, children's ranges and (optionally) the children's cells.
+// P5: final swap(i, n-1), children's ranges and (optionally) the children's cells.
 __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= v.C) return;
@@ -593,10 +708,7 @@ __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split)
     const orb_cell_t cell = v.heap[slot];
     const uint2 rg = v.ranges[slot];
     const uint32_t n = rg.y - rg.x;
-    const uint32_t s = v.part_s[c], ge_tot = v.part_ge[c];
-    uint32_t i = n;
-    if (ge_tot > s) i = min(i, v.tl[rg.x + s]);
-    if (s >= 1) i = min(i, v.tr[rg.x + s - 1]);
+    const uint32_t i = v.part_i[c];
     if (i < n) {
         if (i != n - 1) swap_particles(v, rg.x + i, rg.x + n - 1);
     } else {
@@ -759,9 +871,11 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKResolve:
             k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
-        case kKPartCount: k_part_count<<<grid, kThreads, 0, st>>>(v); break;
-        case kKPartScan: k_part_scan<<<grid_for(v.C, 1, grid), kThreads, 0, st>>>(v); break;
-        case kKPartTables: k_part_tables<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartClassify: k_part_classify<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartScan: k_tile_scan<<<1, 1024, 0, st>>>(v); break;
+        case kKPartCells:
+            k_part_cells<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
+            break;
         case kKPartSwap: k_part_swap<<<grid, kThreads, 0, st>>>(v); break;
         case kKPartFinish:
             k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, arg);
