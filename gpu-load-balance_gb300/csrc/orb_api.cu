@@ -70,7 +70,9 @@ struct orb_ctx {
     DevBuf<uint32_t> tile_off, hist_off, below, part_s, part_i, part_le, out_counts;
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
+    DevBuf<float> edges;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
+    DevBuf<unsigned long long> pt_status;
     DevBuf<int> slots;
     DevBuf<BuildCounters> counters;
     DevBuf<orb_cell_t> staging;
@@ -128,6 +130,7 @@ orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
     ORB_CUDA(ctx->pt_le.ensure(ptiles));
     ORB_CUDA(ctx->pt_ge_pre.ensure(ptiles + 1));
     ORB_CUDA(ctx->pt_le_pre.ensure(ptiles + 1));
+    ORB_CUDA(ctx->pt_status.ensure(ptiles + 1));
     return ORB_OK;
 }
 
@@ -149,6 +152,7 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->iters.ensure(max_cells));
     ORB_CUDA(ctx->slots.ensure(max_cells));
     ORB_CUDA(ctx->hist.ensure(max_bins, true));
+    ORB_CUDA(ctx->edges.ensure(max_bins + max_cells + 16));
     ORB_CUDA(ctx->ptile_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->counters.ensure(1, true));
     return ensure_ptile_buffers(ctx, max_ptiles);
@@ -170,6 +174,7 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.state = ctx->state.p;
     v.iters = ctx->iters.p;
     v.hist = ctx->hist.p;
+    v.edges = ctx->edges.p;
     v.below = ctx->below.p;
     v.ptile_off = ctx->ptile_off.p;
     v.ge_bits = ctx->ge_bits.p;
@@ -178,6 +183,8 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.pt_le = ctx->pt_le.p;
     v.pt_ge_pre = ctx->pt_ge_pre.p;
     v.pt_le_pre = ctx->pt_le_pre.p;
+    v.pt_status = ctx->pt_status.p;
+    v.ticket = &ctx->counters.p->ticket;
     v.part_s = ctx->part_s.p;
     v.part_i = ctx->part_i.p;
     v.part_le = ctx->part_le.p;
@@ -229,8 +236,11 @@ void collect_profile(orb_ctx *ctx) {
 
 void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     const int g = pass_grid(ctx);
+    // look-back state of the tile scan: status words cleared, ticket at zero
+    cudaMemsetAsync(ctx->pt_status.p, 0, ctx->pt_status.cap * sizeof(unsigned long long), ctx->stream);
+    cudaMemsetAsync(&ctx->counters.p->ticket, 0, sizeof(uint32_t), ctx->stream);
     run_kernel(ctx, kKPartClassify, v, g);
-    run_kernel(ctx, kKPartScan, v, 1);
+    run_kernel(ctx, kKPartScan, v, g, (int)(ctx->pt_ge_pre.cap / 1024 + 1));
     run_kernel(ctx, kKPartCells, v, g);
     run_kernel(ctx, kKPartSwap, v, g);
     run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
@@ -331,8 +341,9 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release();
     ctx->part_s.release(); ctx->part_i.release(); ctx->part_le.release(); ctx->out_counts.release();
     ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
+    ctx->edges.release();
     ctx->ptile_off.release(); ctx->ge_bits.release(); ctx->le_bits.release(); ctx->pt_ge.release();
-    ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release();
+    ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release(); ctx->pt_status.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
@@ -399,6 +410,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         v.base = (1 << (l - 1)) - 1;  // src/orbit.cpp:104-107
         v.C = 1 << (l - 1);
         run_kernel(ctx, kKPlan, v, 1);
+        run_kernel(ctx, kKEdges, v, 1);
         st = run_bisection(ctx, v, &passes);
         if (st != ORB_OK) return st;
         partition_level(ctx, v, true);
@@ -423,6 +435,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     ORB_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, sizeof(BuildCounters), cudaMemcpyDeviceToHost, s));
     if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
     ORB_CUDA(cudaStreamSynchronize(s));
+    if (ctx->h_counters->error)
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
     float dev_ms = 0.f;
     ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
     collect_profile(ctx);
@@ -657,11 +671,16 @@ orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells
     orb_status st = service_prepare(ctx, cells, n_cells, true, &v);
     if (st != ORB_OK || n_cells == 0) return st;
     cudaStream_t s = ctx->stream;
+    ORB_CUDA(cudaMemsetAsync(&ctx->counters.p->error, 0, sizeof(uint32_t), s));
     run_kernel(ctx, kKPlan, v, 1);
     partition_level(ctx, v, false);
     ORB_CUDA(cudaGetLastError());
+    ORB_CUDA(cudaMemcpyAsync(&ctx->h_counters->error, &ctx->counters.p->error, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, s));
     ORB_CUDA(cudaStreamSynchronize(s));
     collect_profile(ctx);
+    if (ctx->h_counters->error)
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
     return ORB_OK;
 }
 

@@ -12,7 +12,7 @@ namespace orb {
 static_assert(sizeof(orb_cell_t) == 52, "orb_cell_t must keep the reference's 52-byte Cell layout");
 
 constexpr int kMaxIterations = 32;   // bisection cap, src/orbit.cpp:149
-constexpr int kTile = 8192;          // keys per tile of the count-left passes
+constexpr int kTile = 16384;         // keys per tile of the count-left passes
 constexpr int kPTile = 4096;         // positions per tile of the partition passes
 constexpr int kPWords = kPTile / 32; // bitmask words per partition tile
 constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
@@ -33,6 +33,7 @@ enum Kernel : int {
     kKPartFinish,
     kKCountLeft,
     kKGenerate,
+    kKEdges,
     kNumKernels
 };
 extern const char *const kKernelNames[kNumKernels];
@@ -44,7 +45,9 @@ struct BuildCounters {
     uint32_t unfound;
     uint32_t max_iters;
     uint32_t any_active;  // set by the resolve step when a cell still needs a pass
-    uint32_t pad[3];
+    uint32_t error;       // set when a bounded device wait gave up
+    uint32_t ticket;      // block ticket of the tile scan (reset before each launch)
+    uint32_t pad;
     unsigned long long bytes[16];  // algorithmic bytes per Kernel kind
 };
 
@@ -65,6 +68,7 @@ struct Level {
     uint8_t *state;         // [C]   CellState
     uint8_t *iters;         // [C]   bisection iterations done
     uint32_t *hist;         // histogram pool (kept all-zero between passes)
+    float *edges;           // midpoint-tree edge tables, 2^K + 1 per cell at hist_off[c] + c
     uint32_t *below;        // [C]   keys below the left margin in the current pass
     // partition
     uint32_t *ptile_off;    // [C+1] first partition tile of each cell
@@ -74,6 +78,8 @@ struct Level {
     uint32_t *pt_le;
     uint32_t *pt_ge_pre;    // [ptiles+1] exclusive prefix over all tiles of the level
     uint32_t *pt_le_pre;
+    unsigned long long *pt_status;  // look-back status word per scan block (zeroed per level)
+    uint32_t *ticket;       // block ticket counter of the tile scan
     uint32_t *part_s;       // [C] number of Hoare swaps
     uint32_t *part_i;       // [C] split index (cell-relative); n when clamped
     uint32_t *part_le;      // [C] keys <= cut in the cell

@@ -23,7 +23,7 @@ namespace orb {
 
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
-    "part_cells", "part_swap", "part_finish", "count_left", "generate"};
+    "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_edges"};
 
 namespace {
 
@@ -270,8 +270,43 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
 // ------------------------------------------------------------------------------------
 // Count-left histogram pass
 // ------------------------------------------------------------------------------------
+// In-order edge table of the midpoint tree over [L, R] with 2^K leaves: e[0] = L,
+// e[2^K] = R, and e[j] = mid(e[j - s], e[j + s]) for the node j of stride s, i.e. exactly
+// the cut the reference's bisection computes at that node (src/cell.h:74-76). Built depth
+// by depth by one warp; __syncwarp orders the global writes between depths.
+__device__ void warp_edges(float *e, float L, float R, int K) {
+    const uint32_t nb = 1u << K;
+    const uint32_t lane = threadIdx.x & 31;
+    if (lane == 0) {
+        e[0] = L;
+        e[nb] = R;
+    }
+    __syncwarp();
+    for (int d = 0; d < K; ++d) {
+        const uint32_t stride = nb >> (d + 1);
+        for (uint32_t i = lane; i < (1u << d); i += 32) {
+            const uint32_t j = (2 * i + 1) * stride;
+            e[j] = mid_cut(e[j - stride], e[j + stride]);
+        }
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ float *cell_edges(const Level &v, int c) {
+    return v.edges + v.hist_off[c] + c;
+}
+
+// Edge tables of every cell for the first histogram pass of a level (warp per cell).
+__global__ void __launch_bounds__(kThreads) k_edges(Level v) {
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (c >= v.C) return;
+    const orb_cell_t &cell = v.heap[level_slot(v, c)];
+    warp_edges(cell_edges(v, c), cell.cutMarginLeft, cell.cutMarginRight, v.hist_k[c]);
+}
+
 __global__ void __launch_bounds__(kThreads) k_hist(Level v) {
     __shared__ uint32_t s_hist[1 << kMaxBinsLog2];
+    __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
     const uint32_t total = v.tile_off[v.C];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
@@ -282,23 +317,26 @@ __global__ void __launch_bounds__(kThreads) k_hist(Level v) {
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
         const int K = v.hist_k[tr.c];
         const uint32_t nb = 1u << K;
-        for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) s_hist[b] = 0u;
+        const float *ge = cell_edges(v, tr.c);
+        for (uint32_t j = threadIdx.x; j <= nb; j += blockDim.x) {
+            if (j < nb) s_hist[j] = 0u;
+            s_edge[j] = ge[j];
+        }
         __syncthreads();
+        // First guess from the (nearly uniform) edge spacing, then exact correction against
+        // the edges: bin b holds keys with e[b] <= key < e[b+1].
+        const float scale = __fdividef((float)nb, R - L);
+        const int top = (int)nb - 1;
         uint32_t below = 0;
         for_keys(keys, tr.e0, tr.e1, [&](float k) {
             if (k < L) {
                 ++below;
             } else if (k < R) {
-                float lo = L, hi = R;
-                uint32_t bin = 0;
-                for (int s = 0; s < K; ++s) {
-                    const float m = mid_cut(lo, hi);
-                    const bool right = !(k < m);
-                    bin = (bin << 1) | (uint32_t)right;
-                    lo = right ? m : lo;
-                    hi = right ? hi : m;
-                }
-                atomicAdd(&s_hist[bin], 1u);
+                int g = __float2int_rz((k - L) * scale);
+                g = min(max(g, 0), top);
+                while (k < s_edge[g]) --g;
+                while (!(k < s_edge[g + 1])) ++g;
+                atomicAdd(&s_hist[g], 1u);
             }
         });
         below = block_sum(below, s_red);
@@ -363,6 +401,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
+    if (st == kActive) warp_edges(cell_edges(v, c), L, R, K);  // tree of the next pass
     if (lane == 0) {
         add_bytes(v, kKResolve, 8ull << K);  // bins read and cleared
         cell.cutMarginLeft = L;
@@ -402,19 +441,32 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) 
     return inc - v;
 }
 
-// P1: bitmasks and counts of keys >= cut and keys <= cut per partition tile.
+// Status word of one scan block in the look-back: flag (bits 62-63), count of keys
+// >= cut (bits 31-61) and keys <= cut (bits 0-30). Level totals stay below 2^31.
+constexpr unsigned long long kStAggregate = 1ull << 62;
+constexpr unsigned long long kStInclusive = 2ull << 62;
+constexpr unsigned long long kStFlags = 3ull << 62;
+constexpr uint32_t kLookbackSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned long long pack_status(unsigned long long flag, uint32_t g,
+                                                          uint32_t l) {
+    return flag | ((unsigned long long)g << 31) | (unsigned long long)l;
+}
+
+// P1: bitmasks of keys >= cut and keys <= cut per partition tile, and their counts.
 __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
     __shared__ uint32_t s_cnt[2][kThreads / 32];
     const uint32_t total = v.ptile_off[v.C];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const int c = find_cell(v.ptile_off, v.C, t);
+        const uint32_t t0 = v.ptile_off[c];
         const int slot = level_slot(v, c);
         const orb_cell_t &cell = v.heap[slot];
         const float cut = cell_cut(cell);
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
         const uint2 rg = v.ranges[slot];
-        const uint32_t p0 = rg.x + (t - v.ptile_off[c]) * (uint32_t)kPTile;
+        const uint32_t p0 = rg.x + (t - t0) * (uint32_t)kPTile;
         const uint32_t m = min((uint32_t)kPTile, rg.y - p0);
         uint32_t *gw = v.ge_bits + (size_t)t * kPWords;
         uint32_t *lw = v.le_bits + (size_t)t * kPWords;
@@ -458,36 +510,77 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
     }
 }
 
-// P2: exclusive prefix of the per-tile counts over every tile of the level (one CTA).
-// pt_ge_pre[t] = sum of pt_ge over tiles before t; entry [total] holds the grand total.
-__global__ void __launch_bounds__(1024) k_tile_scan(Level v) {
+// P2: global exclusive prefix of the per-tile counts over every tile of the level:
+// pt_*_pre[t] = sum over tiles before t, entry [total] = grand total. Blocks of 1024 tiles
+// take logical indices by ticket and chain their prefixes with a decoupled look-back (a
+// block only waits on blocks that started before it; the wait is bounded all the same).
+// In-cell prefixes are differences with the cell's first tile.
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) k_tile_scan(Level v) {
     __shared__ uint32_t sh[96];
+    __shared__ uint32_t s_b;
+    __shared__ uint32_t s_pre[2];
     const uint32_t total = v.ptile_off[v.C];
-    const uint32_t per = (total + blockDim.x - 1) / blockDim.x;
-    const uint32_t a0 = min(total, threadIdx.x * per), a1 = min(total, a0 + per);
-    uint32_t sg = 0, sl = 0;
-    for (uint32_t t = a0; t < a1; ++t) {
-        sg += v.pt_ge[t];
-        sl += v.pt_le[t];
+    const uint32_t nblk = total / kScanBlock + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    volatile unsigned long long *status = v.pt_status;
+    if (threadIdx.x == 0) s_b = atomicAdd(v.ticket, 1u);
+    __syncthreads();
+    const uint32_t b = s_b;
+    if (b >= nblk) return;
+    const uint32_t t = b * kScanBlock + threadIdx.x;
+    const uint32_t g = t < total ? v.pt_ge[t] : 0u;
+    const uint32_t l = t < total ? v.pt_le[t] : 0u;
+    uint32_t ag, al;
+    const uint2 ex = block_excl_scan2(g, l, sh, &ag, &al);
+    if (warp == 0) {
+        uint32_t pg = 0, pl = 0;
+        if (b == 0) {
+            if (lane == 0) status[0] = pack_status(kStInclusive, ag, al);
+        } else {
+            if (lane == 0) status[b] = pack_status(kStAggregate, ag, al);
+            long long j = (long long)b - 1;
+            for (;;) {  // 32 predecessors at a time; blocks before 0 count as inclusive zero
+                const long long jj = j - lane;
+                unsigned long long st = kStInclusive;
+                if (jj >= 0) {
+                    uint32_t spins = 0;
+                    while (((st = status[jj]) & kStFlags) == 0ull) {
+                        if (++spins > kLookbackSpinLimit) {
+                            atomicExch(&v.counters->error, 1u);
+                            st = kStInclusive;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                }
+                const uint32_t incl = __ballot_sync(0xffffffffu, (st & kStFlags) == kStInclusive);
+                const int first = incl ? __ffs(incl) - 1 : 32;
+                const bool take = lane <= first;
+                pg += warp_sum(take ? (uint32_t)((st >> 31) & 0x7fffffffull) : 0u);
+                pl += warp_sum(take ? (uint32_t)(st & 0x7fffffffull) : 0u);
+                if (incl) break;
+                j -= 32;
+            }
+            if (lane == 0) status[b] = pack_status(kStInclusive, pg + ag, pl + al);
+        }
+        if (lane == 0) {
+            s_pre[0] = pg;
+            s_pre[1] = pl;
+        }
     }
-    uint32_t tg, tl;
-    uint2 p = block_excl_scan2(sg, sl, sh, &tg, &tl);
-    for (uint32_t t = a0; t < a1; ++t) {
-        const uint32_t g = v.pt_ge[t], l = v.pt_le[t];
-        v.pt_ge_pre[t] = p.x;
-        v.pt_le_pre[t] = p.y;
-        p.x += g;
-        p.y += l;
+    __syncthreads();
+    if (t <= total) {
+        v.pt_ge_pre[t] = s_pre[0] + ex.x;
+        v.pt_le_pre[t] = s_pre[1] + ex.y;
     }
-    if (threadIdx.x == 0) {
-        v.pt_ge_pre[total] = tg;
-        v.pt_le_pre[total] = tl;
-        add_bytes(v, kKPartScan, 16ull * total);
-    }
+    if (threadIdx.x == 0) add_bytes(v, kKPartScan, 16ull * min((uint32_t)kScanBlock, total + 1 - b * kScanBlock));
 }
 
 // Position (cell-relative) of the set bit with in-cell rank `rank` among the bitmasks of
-// tiles [t0, t1) (warp-cooperative; every lane returns the answer).
+// tiles [t0, t1), `pre` the level's global exclusive tile prefix (warp-cooperative; every
+// lane returns the answer).
 __device__ uint32_t warp_select(const uint32_t *bits, const uint32_t *pre, uint32_t t0, uint32_t t1,
                                 uint32_t rank) {
     const int lane = threadIdx.x & 31;
@@ -650,13 +743,12 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
         const int c = find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
         const uint32_t s = v.part_s[c];
-        const uint32_t G0 = v.pt_ge_pre[t0];
+        const uint32_t G0 = v.pt_ge_pre[t0], L0 = v.pt_le_pre[t0];
         const uint32_t ka = v.pt_ge_pre[t] - G0;
         const uint32_t kb = min(s, v.pt_ge_pre[t + 1] - G0);
         if (ka >= kb) continue;
         const uint32_t cnt = kb - ka;
         const uint32_t le_tot = v.part_le[c];
-        const uint32_t L0 = v.pt_le_pre[t0];
         const uint32_t b = v.ranges[level_slot(v, c)].x;
         // left elements: ranks [ka, kb) of this tile's >= mask, in order
         emit_positions(v.ge_bits + (size_t)t * kPWords, ka, ka, kb, (t - t0) * (uint32_t)kPTile,
@@ -676,7 +768,46 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
             emit_positions(v.le_bits + (size_t)u * kPWords, v.pt_le_pre[u] - L0, ra, rb,
                            (u - t0) * (uint32_t)kPTile, true, le_tot - 1 - ka, posR, sh);
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x) swap_particles(v, b + posL[j], b + posR[j]);
+        // four pairs per thread per round: every load is issued before any store
+        constexpr int kB = 4;
+        for (uint32_t j0 = 0; j0 < cnt; j0 += kB * blockDim.x) {
+            uint32_t pa[kB], pb[kB];
+            float xa[kB], xb[kB], ya[kB], yb[kB], za[kB], zb[kB];
+            uint32_t ia[kB], ib[kB];
+#pragma unroll
+            for (int q = 0; q < kB; ++q) {
+                const uint32_t j = j0 + q * blockDim.x + threadIdx.x;
+                const bool ok = j < cnt;
+                pa[q] = ok ? b + posL[j] : 0xffffffffu;
+                pb[q] = ok ? b + posR[j] : 0xffffffffu;
+                if (ok) {
+                    xa[q] = v.x[pa[q]];
+                    xb[q] = v.x[pb[q]];
+                    ya[q] = v.y[pa[q]];
+                    yb[q] = v.y[pb[q]];
+                    za[q] = v.z[pa[q]];
+                    zb[q] = v.z[pb[q]];
+                    if (v.idx) {
+                        ia[q] = v.idx[pa[q]];
+                        ib[q] = v.idx[pb[q]];
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kB; ++q) {
+                if (pa[q] == 0xffffffffu) continue;
+                v.x[pa[q]] = xb[q];
+                v.x[pb[q]] = xa[q];
+                v.y[pa[q]] = yb[q];
+                v.y[pb[q]] = ya[q];
+                v.z[pa[q]] = zb[q];
+                v.z[pb[q]] = za[q];
+                if (v.idx) {
+                    v.idx[pa[q]] = ib[q];
+                    v.idx[pb[q]] = ia[q];
+                }
+            }
+        }
         if (threadIdx.x == 0) add_bytes(v, kKPartSwap, 64ull * cnt);
         __syncthreads();
     }
@@ -868,11 +999,14 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
     switch (k) {
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
         case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKEdges:
+            k_edges<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
+            break;
         case kKResolve:
             k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
         case kKPartClassify: k_part_classify<<<grid, kThreads, 0, st>>>(v); break;
-        case kKPartScan: k_tile_scan<<<1, 1024, 0, st>>>(v); break;
+        case kKPartScan: k_tile_scan<<<arg, kScanBlock, 0, st>>>(v); break;
         case kKPartCells:
             k_part_cells<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
