@@ -67,7 +67,7 @@ struct orb_ctx {
     DevBuf<uint32_t> idx;
     DevBuf<orb_cell_t> heap;
     DevBuf<uint2> ranges;
-    DevBuf<uint32_t> tile_off, hist_off, below, part_s, part_i, part_le, out_counts;
+    DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
     DevBuf<float> edges;
@@ -143,6 +143,7 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->tile_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->hist_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->below.ensure(max_cells));
+    ORB_CUDA(ctx->inb.ensure(max_cells));
     ORB_CUDA(ctx->part_s.ensure(max_cells));
     ORB_CUDA(ctx->part_i.ensure(max_cells));
     ORB_CUDA(ctx->part_le.ensure(max_cells));
@@ -176,6 +177,7 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.hist = ctx->hist.p;
     v.edges = ctx->edges.p;
     v.below = ctx->below.p;
+    v.inb = ctx->inb.p;
     v.ptile_off = ctx->ptile_off.p;
     v.ge_bits = ctx->ge_bits.p;
     v.le_bits = ctx->le_bits.p;
@@ -338,7 +340,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->x.release(); ctx->y.release(); ctx->z.release();
     ctx->idx.release();
     ctx->heap.release(); ctx->ranges.release();
-    ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release();
+    ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release(); ctx->inb.release();
     ctx->part_s.release(); ctx->part_i.release(); ctx->part_le.release(); ctx->out_counts.release();
     ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
     ctx->edges.release();

@@ -70,6 +70,7 @@ struct Level {
     uint32_t *hist;         // histogram pool (kept all-zero between passes)
     float *edges;           // midpoint-tree edge tables, 2^K + 1 per cell at hist_off[c] + c
     uint32_t *below;        // [C]   keys below the left margin in the current pass
+    uint32_t *inb;          // [C]   keys inside the current bracket (n before the first pass)
     // partition
     uint32_t *ptile_off;    // [C+1] first partition tile of each cell
     uint32_t *ge_bits;      // [ptiles * kPWords] bit p: key >= cut

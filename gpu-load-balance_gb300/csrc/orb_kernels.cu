@@ -257,6 +257,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
         v.state[c] = kActive;
         v.iters[c] = 0;
         v.below[c] = 0;
+        v.inb[c] = n;
         p.x += (n + kTile - 1) / kTile;
         p.y += 1u << k;
     }
@@ -304,7 +305,38 @@ __global__ void __launch_bounds__(kThreads) k_edges(Level v) {
     warp_edges(cell_edges(v, c), cell.cutMarginLeft, cell.cutMarginRight, v.hist_k[c]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_hist(Level v) {
+// Bin of key k (L <= k < R) in the edge table e[0..nb]: the largest b with e[b] <= k, i.e.
+// the leaf the bisection's descent reaches. The spacing of the edges is uniform to a few
+// ulps, so the scaled guess is off by at most one except in brackets only a few ulps
+// wide, which fall back to a binary search over the table.
+template <class EdgeAt>
+__device__ __forceinline__ int edge_bin(float k, float L, float scale, int top, EdgeAt e) {
+    int g = __float2int_rz((k - L) * scale);
+    g = min(max(g, 0), top);
+    if (k < e(g)) {
+        --g;
+        if (g >= 0 && !(k < e(g))) return g;
+    } else if (!(k < e(g + 1))) {
+        ++g;
+        if (g <= top && k < e(g + 1)) return g;
+    } else {
+        return g;
+    }
+    int lo = 0, hi = top;  // largest b in [0, top] with e(b) <= k (e(0) = L <= k)
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (e(mid) <= k)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Keys per thread per round of the histogram pass (float4 loads issued together).
+constexpr int kHistVec = 4;
+
+__global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
     __shared__ uint32_t s_hist[1 << kMaxBinsLog2];
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
@@ -317,39 +349,70 @@ __global__ void __launch_bounds__(kThreads) k_hist(Level v) {
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
         const int K = v.hist_k[tr.c];
         const uint32_t nb = 1u << K;
-        const float *ge = cell_edges(v, tr.c);
-        for (uint32_t j = threadIdx.x; j <= nb; j += blockDim.x) {
-            if (j < nb) s_hist[j] = 0u;
-            s_edge[j] = ge[j];
-        }
-        __syncthreads();
-        // First guess from the (nearly uniform) edge spacing, then exact correction against
-        // the edges: bin b holds keys with e[b] <= key < e[b+1].
-        const float scale = __fdividef((float)nb, R - L);
         const int top = (int)nb - 1;
+        const float scale = __fdividef((float)nb, R - L);
+        const float *ge = cell_edges(v, tr.c);
+        uint32_t *gh = v.hist + v.hist_off[tr.c];
+        // Sparse pass: few keys of the cell lie in the bracket (known from the previous
+        // pass), so they go straight to the global bins; dense pass: shared-memory bins.
+        const uint32_t cell_tiles = v.tile_off[tr.c + 1] - v.tile_off[tr.c];
+        const bool sparse = v.inb[tr.c] <= 64u * cell_tiles;
+        if (!sparse) {
+            for (uint32_t j = threadIdx.x; j <= nb; j += blockDim.x) {
+                if (j < nb) s_hist[j] = 0u;
+                s_edge[j] = ge[j];
+            }
+            __syncthreads();
+        }
         uint32_t below = 0;
-        for_keys(keys, tr.e0, tr.e1, [&](float k) {
+        auto visit = [&](float k) {
             if (k < L) {
                 ++below;
             } else if (k < R) {
-                int g = __float2int_rz((k - L) * scale);
-                g = min(max(g, 0), top);
-                while (k < s_edge[g]) --g;
-                while (!(k < s_edge[g + 1])) ++g;
-                atomicAdd(&s_hist[g], 1u);
+                if (sparse) {
+                    const int g = edge_bin(k, L, scale, top, [&](int j) { return __ldg(ge + j); });
+                    atomicAdd(&gh[g], 1u);
+                } else {
+                    const int g = edge_bin(k, L, scale, top, [&](int j) { return s_edge[j]; });
+                    atomicAdd(&s_hist[g], 1u);
+                }
             }
-        });
+        };
+        // keys [e0, e1): scalar head to 16-byte alignment, float4 body, scalar tail
+        const uint32_t e0 = tr.e0, e1 = tr.e1;
+        const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
+        const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
+        for (uint32_t i = e0 + threadIdx.x; i < a0; i += blockDim.x) visit(__ldg(keys + i));
+        const uint32_t n4 = (e1 - a0) >> 2;
+        const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
+        for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * blockDim.x) {
+            float4 q[kHistVec];
+#pragma unroll
+            for (int u = 0; u < kHistVec; ++u) {
+                const uint32_t j = j0 + u * blockDim.x + threadIdx.x;
+                q[u] = j < n4 ? __ldg(k4 + j) : make_float4(R, R, R, R);  // R: never counted
+            }
+#pragma unroll
+            for (int u = 0; u < kHistVec; ++u) {
+                visit(q[u].x);
+                visit(q[u].y);
+                visit(q[u].z);
+                visit(q[u].w);
+            }
+        }
+        for (uint32_t i = a0 + (n4 << 2) + threadIdx.x; i < e1; i += blockDim.x) visit(__ldg(keys + i));
         below = block_sum(below, s_red);
         if (threadIdx.x == 0) {
             if (below) atomicAdd(&v.below[tr.c], below);
-            add_bytes(v, kKHist, 4ull * (tr.e1 - tr.e0));
+            add_bytes(v, kKHist, 4ull * (e1 - e0));
         }
-        uint32_t *g = v.hist + v.hist_off[tr.c];
-        for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-            const uint32_t h = s_hist[b];
-            if (h) atomicAdd(&g[b], h);
+        if (!sparse) {
+            for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+                const uint32_t h = s_hist[b];
+                if (h) atomicAdd(&gh[b], h);
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -399,9 +462,13 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         width = half;
     }
     if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
+    const uint32_t next_inb = g[pos];  // keys in the bracket the next pass would bin
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
-    if (st == kActive) warp_edges(cell_edges(v, c), L, R, K);  // tree of the next pass
+    if (st == kActive) {
+        if (lane == 0) v.inb[c] = next_inb;
+        warp_edges(cell_edges(v, c), L, R, K);  // tree of the next pass
+    }
     if (lane == 0) {
         add_bytes(v, kKResolve, 8ull << K);  // bins read and cleared
         cell.cutMarginLeft = L;
