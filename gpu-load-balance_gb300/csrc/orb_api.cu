@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -68,6 +69,8 @@ struct orb_ctx {
     DevBuf<orb_cell_t> heap;
     DevBuf<uint2> ranges;
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
+    DevBuf<uint32_t> htile_cell, ptile_cell;
+    int cta_min_cells = 0;  // levels with at least this many cells bisect one cell per CTA
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
     DevBuf<float> edges;
@@ -124,6 +127,7 @@ bool is_device_ptr(const void *p) {
 }
 
 orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
+    ORB_CUDA(ctx->ptile_cell.ensure(ptiles));
     ORB_CUDA(ctx->ge_bits.ensure(ptiles * kPWords));
     ORB_CUDA(ctx->le_bits.ensure(ptiles * kPWords));
     ORB_CUDA(ctx->pt_ge.ensure(ptiles));
@@ -141,6 +145,7 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->heap.ensure(heap_cells));
     ORB_CUDA(ctx->ranges.ensure(heap_cells));
     ORB_CUDA(ctx->tile_off.ensure(max_cells + 1));
+    ORB_CUDA(ctx->htile_cell.ensure(n / kTile + max_cells + 2));
     ORB_CUDA(ctx->hist_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->below.ensure(max_cells));
     ORB_CUDA(ctx->inb.ensure(max_cells));
@@ -170,6 +175,8 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.ranges = ctx->ranges.p;
     v.slots = nullptr;
     v.tile_off = ctx->tile_off.p;
+    v.htile_cell = ctx->htile_cell.p;
+    v.ptile_cell = ctx->ptile_cell.p;
     v.hist_off = ctx->hist_off.p;
     v.hist_k = ctx->hist_k.p;
     v.state = ctx->state.p;
@@ -311,6 +318,16 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
         for (auto &ev : ctx->ev)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) { st = cuda_fail(ctx, e, "cudaEventCreate"); break; }
         if (st != ORB_OK) break;
+        if ((e = configure_kernels()) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "cudaFuncSetAttribute");
+            break;
+        }
+        {
+            const char *env = std::getenv("ORB_CTA_MIN_CELLS");
+            // Measured on GB300 (2^27 particles, 2^16 leaves): the multi-CTA histogram passes
+            // beat one-CTA-per-cell at every level, so the CTA path is opt-in.
+            ctx->cta_min_cells = env ? std::atoi(env) : 1 << 30;
+        }
         if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess) {
             st = cuda_fail(ctx, e, "cudaMallocHost");
             break;
@@ -347,6 +364,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->ptile_off.release(); ctx->ge_bits.release(); ctx->le_bits.release(); ctx->pt_ge.release();
     ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release(); ctx->pt_status.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
+    ctx->htile_cell.release(); ctx->ptile_cell.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
@@ -412,8 +430,14 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         v.base = (1 << (l - 1)) - 1;  // src/orbit.cpp:104-107
         v.C = 1 << (l - 1);
         run_kernel(ctx, kKPlan, v, 1);
-        run_kernel(ctx, kKEdges, v, 1);
-        st = run_bisection(ctx, v, &passes);
+        run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
+        if (v.C >= ctx->cta_min_cells) {
+            // many cells: one CTA bisects one cell, no host round trip
+            run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
+        } else {
+            run_kernel(ctx, kKEdges, v, 1);
+            st = run_bisection(ctx, v, &passes);
+        }
         if (st != ORB_OK) return st;
         partition_level(ctx, v, true);
         ORB_CUDA(cudaGetLastError());
@@ -654,6 +678,7 @@ orb_status orb_count_left(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cell
     cudaStream_t s = ctx->stream;
     ORB_CUDA(cudaMemsetAsync(ctx->out_counts.p, 0, n_cells * sizeof(uint32_t), s));
     run_kernel(ctx, kKPlan, v, 1);
+    run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
     run_kernel(ctx, kKCountLeft, v, pass_grid(ctx));
     ORB_CUDA(cudaGetLastError());
     std::vector<uint32_t> res(n_cells);
@@ -675,6 +700,7 @@ orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells
     cudaStream_t s = ctx->stream;
     ORB_CUDA(cudaMemsetAsync(&ctx->counters.p->error, 0, sizeof(uint32_t), s));
     run_kernel(ctx, kKPlan, v, 1);
+    run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
     partition_level(ctx, v, false);
     ORB_CUDA(cudaGetLastError());
     ORB_CUDA(cudaMemcpyAsync(&ctx->h_counters->error, &ctx->counters.p->error, sizeof(uint32_t),

@@ -34,6 +34,8 @@ enum Kernel : int {
     kKCountLeft,
     kKGenerate,
     kKEdges,
+    kKBisectCta,
+    kKTileMap,
     kNumKernels
 };
 extern const char *const kKernelNames[kNumKernels];
@@ -63,6 +65,8 @@ struct Level {
     int C;
     // plan
     uint32_t *tile_off;     // [C+1] first tile of each cell
+    uint32_t *htile_cell;   // [tiles] cell of each count-left tile (null: binary search)
+    uint32_t *ptile_cell;   // [ptiles] cell of each partition tile (null: binary search)
     uint32_t *hist_off;     // [C+1] first bin of each cell in the histogram pool
     uint8_t *hist_k;        // [C]   tree depth of each cell's histogram
     uint8_t *state;         // [C]   CellState
@@ -117,6 +121,7 @@ __device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {
 void launch_init(const Level &v, uint64_t n, const float lower[3], const float upper[3],
                  uint32_t d, int heap_cells, cudaStream_t st);
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st);
+cudaError_t configure_kernels();  // once per device (dynamic shared memory limits)
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);
 void launch_gen_plummer(uint64_t seed, uint64_t n, const float *centres, const double *scales,

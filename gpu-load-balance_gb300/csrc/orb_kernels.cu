@@ -23,7 +23,8 @@ namespace orb {
 
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
-    "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_edges"};
+    "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_edges",
+    "bisect_cta", "tile_map"};
 
 namespace {
 
@@ -176,7 +177,7 @@ struct TileRef {
 
 __device__ __forceinline__ TileRef tile_ref(const Level &v, uint32_t t) {
     TileRef r;
-    r.c = find_cell(v.tile_off, v.C, t);
+    r.c = v.htile_cell ? (int)v.htile_cell[t] : find_cell(v.tile_off, v.C, t);
     r.slot = level_slot(v, r.c);
     r.local = t - v.tile_off[r.c];
     const uint2 rg = v.ranges[r.slot];
@@ -484,6 +485,209 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
 }
 
 // ------------------------------------------------------------------------------------
+// Bisection with one CTA per cell, for levels with many cells (no multi-CTA passes, no
+// global histograms, no host round trip). Every round bins the candidate keys of the cell
+// into a shared-memory midpoint tree and replays up to K iterations of the reference loop
+// (src/orbit.cpp:146-232) on it; then the keys of the remaining bracket become the
+// candidates of the next round. Candidates start as the cell's keys in global memory, or
+// in the shared list when they fit; as soon as the bracket fits the list it is compacted
+// into it. `base` counts the keys already known to lie below L. Same cuts, same integer
+// counts, same float test as the reference.
+// ------------------------------------------------------------------------------------
+constexpr int kCtaThreads = 512;
+constexpr uint32_t kListCap = 8192;                     // shared list of candidate keys
+constexpr uint32_t kListPerThread = kListCap / kCtaThreads;
+constexpr size_t kCtaSmemBytes = kListCap * sizeof(float) +
+                                 (1u << kMaxBinsLog2) * sizeof(uint32_t) +
+                                 ((1u << kMaxBinsLog2) + 1) * sizeof(float);
+
+__global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
+    extern __shared__ __align__(16) unsigned char cta_smem[];
+    float *list = reinterpret_cast<float *>(cta_smem);
+    uint32_t *s_hist = reinterpret_cast<uint32_t *>(list + kListCap);
+    float *s_edge = reinterpret_cast<float *>(s_hist + (1u << kMaxBinsLog2));
+    __shared__ uint32_t sh[96];
+    __shared__ uint32_t s_fill;
+    const uint32_t tid = threadIdx.x;
+    constexpr uint32_t kBins = 1u << kMaxBinsLog2;
+    for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
+        const int slot = level_slot(v, c);
+        orb_cell_t &cell = v.heap[slot];
+        const uint2 rg = v.ranges[slot];
+        const uint32_t n = rg.y - rg.x;
+        const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+        float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+        uint32_t it = 0, base = 0, m = n, inb = n;
+        int st = kActive;
+        bool in_list = n <= kListCap;
+        unsigned long long bytes = 0;
+        if (in_list) {
+            for (uint32_t i = tid; i < n; i += blockDim.x) list[i] = __ldg(keys + rg.x + i);
+            bytes += 4ull * n;
+        }
+        for (;;) {
+            // ---- histogram round over the candidates, tree depth from their count
+            const uint32_t cand = in_list ? m : inb;
+            const int K = max(1, min(kMaxBinsLog2, 32 - __clz(max(cand, 1u))));
+            const uint32_t nb = 1u << K;
+            for (uint32_t j = tid; j < kBins; j += blockDim.x) s_hist[j] = 0u;
+            for (uint32_t j = tid; j <= nb; j += blockDim.x) {
+                float e;
+                if (j == 0) {
+                    e = L;
+                } else if (j == nb) {
+                    e = R;
+                } else {
+                    float lo = L, hi = R;
+                    uint32_t b0 = 0, span = nb;
+                    for (;;) {
+                        const uint32_t half = span >> 1;
+                        const float mm = mid_cut(lo, hi);
+                        const uint32_t idx = b0 + half;
+                        if (j == idx) {
+                            e = mm;
+                            break;
+                        }
+                        if (j < idx) {
+                            hi = mm;
+                        } else {
+                            lo = mm;
+                            b0 = idx;
+                        }
+                        span = half;
+                    }
+                }
+                s_edge[j] = e;
+            }
+            __syncthreads();
+            const float scale = __fdividef((float)nb, R - L);
+            uint32_t below = 0;
+            auto visit = [&](float k) {
+                if (k < L) {
+                    ++below;
+                } else if (k < R) {
+                    const int g = edge_bin(k, L, scale, (int)nb - 1, [&](int j) { return s_edge[j]; });
+                    atomicAdd(&s_hist[g], 1u);
+                }
+            };
+            if (in_list) {
+                for (uint32_t i = tid; i < m; i += blockDim.x) visit(list[i]);
+            } else {
+                for_keys(keys, rg.x, rg.y, visit);
+                bytes += 4ull * n;
+            }
+            below = base + block_sum(below, sh);
+            // exclusive prefix of the bins in place (4 bins per thread)
+            uint32_t h4[4], loc = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                h4[q] = s_hist[tid * 4 + q];
+                loc += h4[q];
+            }
+            uint32_t tot_a, tot_b;
+            const uint2 ex = block_excl_scan2(loc, 0u, sh, &tot_a, &tot_b);
+            uint32_t run = ex.x;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                s_hist[tid * 4 + q] = run;
+                run += h4[q];
+            }
+            __syncthreads();
+            // ---- replay up to K iterations (identically in every thread)
+            uint32_t pos = 0, width = nb;
+            for (int step = 0; step < K; ++step) {
+                if (it >= (uint32_t)kMaxIterations) {
+                    st = kCapped;
+                    break;
+                }
+                const uint32_t half = width >> 1;
+                const uint32_t cl = below + s_hist[pos + half];
+                ++it;
+                const int dir = convergence(cl, n);
+                if (dir == 0) {
+                    st = kFound;
+                    break;
+                }
+                const float cut = mid_cut(L, R);
+                if (dir > 0) {
+                    R = cut;
+                } else {
+                    L = cut;
+                    pos += half;
+                }
+                width = half;
+            }
+            if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
+            if (st != kActive) break;
+            inb = s_hist[pos + 1] - s_hist[pos];  // keys in the new bracket [L, R)
+            __syncthreads();
+            // ---- the new bracket's keys become the candidates
+            if (in_list) {
+                // every thread reads its keys, then (after the barrier in block_sum) the
+                // keys of the new bracket are appended, one warp-aggregated slot per round
+                float kq[kListPerThread];
+                uint32_t blw = 0;
+#pragma unroll
+                for (uint32_t q = 0; q < kListPerThread; ++q) {
+                    const uint32_t i = tid + q * kCtaThreads;
+                    kq[q] = i < m ? list[i] : R;  // R: neither below L nor kept
+                    blw += kq[q] < L;
+                }
+                if (tid == 0) s_fill = 0;
+                base += block_sum(blw, sh);
+                const uint32_t lane = tid & 31;
+#pragma unroll
+                for (uint32_t q = 0; q < kListPerThread; ++q) {
+                    const bool keep = !(kq[q] < L) && kq[q] < R;
+                    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+                    uint32_t wb = 0;
+                    if (lane == 0 && bal) wb = atomicAdd(&s_fill, (uint32_t)__popc(bal));
+                    wb = __shfl_sync(0xffffffffu, wb, 0);
+                    if (keep) list[wb + __popc(bal & ((1u << lane) - 1u))] = kq[q];
+                }
+                __syncthreads();
+                m = s_fill;
+            } else if (inb <= kListCap) {
+                if (tid == 0) s_fill = 0;
+                __syncthreads();
+                uint32_t blw = 0;
+                for_keys(keys, rg.x, rg.y, [&](float k) {
+                    if (k < L)
+                        ++blw;
+                    else if (k < R)
+                        list[atomicAdd(&s_fill, 1u)] = k;
+                });
+                bytes += 4ull * n;
+                base = block_sum(blw, sh);
+                m = s_fill;
+                in_list = true;
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            cell.cutMarginLeft = L;
+            cell.cutMarginRight = R;
+            cell.foundCut = st == kFound ? 1 : 0;
+            v.iters[c] = (uint8_t)it;
+            v.state[c] = (uint8_t)st;
+            atomicMax(&v.counters->max_iters, it);
+            if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+            add_bytes(v, kKBisectCta, bytes);
+        }
+        __syncthreads();
+    }
+}
+
+// Tile -> cell maps of the level (one binary search per tile, once per level).
+__global__ void k_tile_map(Level v) {
+    const uint32_t ht = v.tile_off[v.C], pt = v.ptile_off[v.C];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < max(ht, pt); t += gridDim.x * blockDim.x) {
+        if (t < ht) v.htile_cell[t] = find_cell(v.tile_off, v.C, t);
+        if (t < pt) v.ptile_cell[t] = find_cell(v.ptile_off, v.C, t);
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // Partition
 //
 // Partition tiles are kPTile consecutive positions of one cell. Per tile, the classify
@@ -526,7 +730,7 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
     const uint32_t total = v.ptile_off[v.C];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const int c = find_cell(v.ptile_off, v.C, t);
+        const int c = v.ptile_cell ? (int)v.ptile_cell[t] : find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c];
         const int slot = level_slot(v, c);
         const orb_cell_t &cell = v.heap[slot];
@@ -807,7 +1011,7 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
     __shared__ uint32_t sh[96];
     const uint32_t total = v.ptile_off[v.C];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const int c = find_cell(v.ptile_off, v.C, t);
+        const int c = v.ptile_cell ? (int)v.ptile_cell[t] : find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
         const uint32_t s = v.part_s[c];
         const uint32_t G0 = v.pt_ge_pre[t0], L0 = v.pt_le_pre[t0];
@@ -1066,6 +1270,10 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
     switch (k) {
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
         case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKBisectCta:
+            k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
+            break;
+        case kKTileMap: k_tile_map<<<grid, kThreads, 0, st>>>(v); break;
         case kKEdges:
             k_edges<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
@@ -1084,6 +1292,11 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKCountLeft: k_count_left<<<grid, kThreads, 0, st>>>(v); break;
         default: break;
     }
+}
+
+cudaError_t configure_kernels() {
+    return cudaFuncSetAttribute(k_bisect_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kCtaSmemBytes);
 }
 
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,

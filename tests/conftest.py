@@ -35,3 +35,24 @@ def ctx(engine):
     c = engine.Context(0)
     yield c
     c.close()
+
+
+def _context_with(engine, cta_min_cells):
+    old = os.environ.get("ORB_CTA_MIN_CELLS")
+    os.environ["ORB_CTA_MIN_CELLS"] = str(cta_min_cells)
+    try:
+        return engine.Context(0)
+    finally:
+        if old is None:
+            del os.environ["ORB_CTA_MIN_CELLS"]
+        else:
+            os.environ["ORB_CTA_MIN_CELLS"] = old
+
+
+@pytest.fixture(scope="session", params=["multi_cta", "cta_per_cell"])
+def any_ctx(request, engine):
+    """A context forced onto one bisection path for every level: the multi-CTA histogram
+    passes, or one CTA per cell."""
+    c = _context_with(engine, 1 << 30 if request.param == "multi_cta" else 1)
+    yield c
+    c.close()

@@ -49,9 +49,9 @@ def test_generator_bit_exact(ctx, engine, oracle, kind):
 
 @pytest.mark.parametrize("n,d,seed", [(1 << 12, 1 << 4, 1), (1 << 16, 1 << 8, 2),
                                       ((1 << 16) + 123, 1 << 9, 3), (50000, 1 << 12, 4)])
-def test_uniform_parity(ctx, oracle, n, d, seed):
+def test_uniform_parity(any_ctx, oracle, n, d, seed):
     x, y, z = oracle.gen_uniform(seed, n)
-    run_both(ctx, oracle, x, y, z, d)
+    run_both(any_ctx, oracle, x, y, z, d)
 
 
 def test_config1_parity(ctx, oracle):
@@ -62,52 +62,56 @@ def test_config1_parity(ctx, oracle):
 
 
 @pytest.mark.parametrize("n,d,seed", [(1 << 16, 1 << 10, 5), (1 << 18, 1 << 12, 6)])
-def test_plummer_parity(ctx, oracle, n, d, seed):
+def test_plummer_parity(any_ctx, oracle, n, d, seed):
     x, y, z = oracle.gen_plummer(seed, n)
-    run_both(ctx, oracle, x, y, z, d)
+    run_both(any_ctx, oracle, x, y, z, d)
 
 
-def test_tie_heavy_parity(ctx, oracle):
+def test_tie_heavy_parity(any_ctx, oracle):
     """Coordinates on a 64-value grid: most cuts land on keys, Hoare tie placement decides
     membership."""
     rng = np.random.default_rng(7)
     n = 1 << 17
     x, y, z = ((rng.integers(0, 64, n).astype(np.float32) / np.float32(64) - np.float32(0.5))
                for _ in range(3))
-    res, ref = run_both(ctx, oracle, x, y, z, 1 << 10)
+    res, ref = run_both(any_ctx, oracle, x, y, z, 1 << 10)
     assert ref.stats["unfound_cells"] > 0  # the grid defeats the bisection somewhere
 
 
-def test_small_and_degenerate_cells(ctx, oracle):
+def test_small_and_degenerate_cells(any_ctx, oracle):
     rng = np.random.default_rng(8)
     for n in (0, 1, 2, 3, 5, 7, 17, 100):
         for d in (1, 2, 4, 16):
             x, y, z = (rng.random(n).astype(np.float32) - np.float32(0.5) for _ in range(3))
-            run_both(ctx, oracle, x, y, z, d)
+            run_both(any_ctx, oracle, x, y, z, d)
 
 
-def test_duplicates_nan_out_of_box(ctx, oracle):
+def test_duplicates_nan_out_of_box(any_ctx, oracle):
     n = 4096
     same = np.full(n, 0.25, np.float32)
-    run_both(ctx, oracle, same, same.copy(), same.copy(), 8)
+    run_both(any_ctx, oracle, same, same.copy(), same.copy(), 8)
+    # a bracket that never shrinks below the shared list: repeated histogram passes
+    big = np.full(40000, -0.125, np.float32)
+    big[::7] = 0.3
+    run_both(any_ctx, oracle, big, big.copy(), big[::-1].copy(), 4)
     rng = np.random.default_rng(9)
     x = rng.random(n).astype(np.float32) - np.float32(0.5)
     x[rng.integers(0, n, 200)] = np.nan
     y = rng.random(n).astype(np.float32) * np.float32(4) - np.float32(2)  # out of the box
     z = np.round(rng.random(n).astype(np.float32) * 8) / np.float32(8) - np.float32(0.5)
-    run_both(ctx, oracle, x, y, z, 64)
+    run_both(any_ctx, oracle, x, y, z, 64)
 
 
-def test_reference_level_bound(ctx, oracle):
+def test_reference_level_bound(any_ctx, oracle):
     """levels = log2(d)-1 is the reference driver's own loop (d/2 leaves)."""
     x, y, z = oracle.gen_uniform(10, 1 << 15)
-    run_both(ctx, oracle, x, y, z, 1 << 8, levels=7)
+    run_both(any_ctx, oracle, x, y, z, 1 << 8, levels=7)
 
 
-def test_custom_box(ctx, oracle):
+def test_custom_box(any_ctx, oracle):
     x, y, z = oracle.gen_uniform(12, 1 << 14)
     x = x * np.float32(3)
-    run_both(ctx, oracle, x, y, z, 1 << 6, lower=(-1.5, -0.5, -0.5), upper=(1.5, 0.5, 0.5))
+    run_both(any_ctx, oracle, x, y, z, 1 << 6, lower=(-1.5, -0.5, -0.5), upper=(1.5, 0.5, 0.5))
 
 
 def test_device_pointers(ctx, oracle):
