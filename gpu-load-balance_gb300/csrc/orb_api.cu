@@ -79,6 +79,8 @@ struct orb_ctx {
     DevBuf<int> slots;
     DevBuf<BuildCounters> counters;
     DevBuf<orb_cell_t> staging;
+    DevBuf<BatchRoot> batch_roots;
+    DevBuf<int> batch_slots;
     BuildCounters *h_counters = nullptr;  // pinned
 
     // service layer state
@@ -272,6 +274,39 @@ orb_status run_bisection(orb_ctx *ctx, const Level &v, uint32_t *passes) {
     return ORB_OK;
 }
 
+// One level of the tree: heap slots [base, base + C) or the explicit slot list `slots`.
+struct LevelDesc {
+    int base;
+    const int *slots;
+    int C;
+};
+
+// The reference's level loop (src/orbit.cpp:102-275) over every cell of every level: plan,
+// bisection (one warp for small cells, one CTA per cell or the multi-CTA histogram passes
+// for the rest), partition and split.
+orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes) {
+    for (const LevelDesc &d : lv) {
+        v.base = d.base;
+        v.slots = d.slots;
+        v.C = d.C;
+        if (v.C == 0) continue;
+        run_kernel(ctx, kKPlan, v, 1);
+        run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
+        if (v.C >= ctx->cta_min_cells) {
+            // many cells: one CTA bisects one cell, no host round trip
+            run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
+        } else {
+            run_kernel(ctx, kKBisectWarp, v, 1);  // cells small enough for one warp
+            run_kernel(ctx, kKEdges, v, 1);
+            orb_status st = run_bisection(ctx, v, passes);
+            if (st != ORB_OK) return st;
+        }
+        partition_level(ctx, v, true);
+        ORB_CUDA(cudaGetLastError());
+    }
+    return ORB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -365,6 +400,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release(); ctx->pt_status.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     ctx->htile_cell.release(); ctx->ptile_cell.release();
+    ctx->batch_roots.release(); ctx->batch_slots.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
@@ -426,22 +462,11 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     launch_init(v, n, lower, upper, d, (int)heap_cells, s);
     ORB_CUDA(cudaGetLastError());
     uint32_t passes = 0;
-    for (uint32_t l = 1; l <= levels; ++l) {
-        v.base = (1 << (l - 1)) - 1;  // src/orbit.cpp:104-107
-        v.C = 1 << (l - 1);
-        run_kernel(ctx, kKPlan, v, 1);
-        run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
-        if (v.C >= ctx->cta_min_cells) {
-            // many cells: one CTA bisects one cell, no host round trip
-            run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
-        } else {
-            run_kernel(ctx, kKEdges, v, 1);
-            st = run_bisection(ctx, v, &passes);
-        }
-        if (st != ORB_OK) return st;
-        partition_level(ctx, v, true);
-        ORB_CUDA(cudaGetLastError());
-    }
+    std::vector<LevelDesc> lv;
+    for (uint32_t l = 1; l <= levels; ++l)
+        lv.push_back({(1 << (l - 1)) - 1, nullptr, 1 << (l - 1)});  // src/orbit.cpp:104-107
+    st = run_levels(ctx, v, lv, &passes);
+    if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (!dev) {
         ORB_CUDA(cudaStreamSynchronize(s));
@@ -734,6 +759,160 @@ orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells
     ORB_CUDA(cudaSetDevice(ctx->device));
     ORB_CUDA(cudaMemcpyAsync(ctx->ranges.p, ranges, n_cells * sizeof(uint2), cudaMemcpyHostToDevice, ctx->stream));
     ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ORB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched builds
+// ---------------------------------------------------------------------------------------
+orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                           const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
+                           uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                           orb_build_info *info) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
+    if ((n_total > 0 && (!x || !y || !z)) || (k > 0 && (!inst || !heaps || !ranges)))
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
+    if (n_total >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "n_total must be below 2^31");
+    const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
+    if (dev && n_total > 0 && (!is_device_ptr(x) || !is_device_ptr(y) || !is_device_ptr(z) ||
+                               (perm && !is_device_ptr(perm))))
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "ORB_DEVICE_POINTERS set but a pointer is not device memory");
+    // validate instances, heap bases, per-level slot lists
+    std::vector<BatchRoot> roots(k);
+    std::vector<uint32_t> lev(k);
+    uint64_t heap_cells = 0;
+    uint32_t max_levels = 0;
+    std::vector<std::pair<uint64_t, uint64_t>> spans;
+    for (uint32_t i = 0; i < k; ++i) {
+        const orb_batch_instance &b = inst[i];
+        if (b.d == 0 || (b.d & (b.d - 1)) != 0 || b.d > (1u << 30))
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance d must be a power of two");
+        if (b.offset + b.n > n_total) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance outside the arrays");
+        const int ylev = log2_exact(b.d);
+        const uint32_t L = b.levels ? b.levels : (uint32_t)ylev;
+        if ((int)L > ylev) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance levels exceeds log2(d)");
+        lev[i] = L;
+        max_levels = std::max(max_levels, L);
+        BatchRoot &r = roots[i];
+        r.offset = (uint32_t)b.offset;
+        r.n = (uint32_t)b.n;
+        r.d = b.d;
+        r.heap_base = (uint32_t)heap_cells;
+        for (int a = 0; a < 3; ++a) {
+            r.lower[a] = b.lower[a];
+            r.upper[a] = b.upper[a];
+        }
+        heap_cells += 2ull * b.d - 1;
+        if (b.n) spans.emplace_back(b.offset, b.offset + b.n);
+    }
+    if (heap_cells >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "too many cells");
+    std::sort(spans.begin(), spans.end());
+    for (size_t i = 1; i < spans.size(); ++i)
+        if (spans[i].first < spans[i - 1].second)
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instances overlap");
+    std::vector<int> slots;
+    std::vector<LevelDesc> lv;
+    std::vector<size_t> lv_off;
+    uint32_t max_cells = 1;
+    for (uint32_t l = 1; l <= max_levels; ++l) {
+        lv_off.push_back(slots.size());
+        for (uint32_t i = 0; i < k; ++i) {
+            if (lev[i] < l) continue;
+            const int first = (int)roots[i].heap_base + (1 << (l - 1)) - 1;
+            for (int j = 0; j < (1 << (l - 1)); ++j) slots.push_back(first + j);
+        }
+        max_cells = std::max<uint32_t>(max_cells, (uint32_t)(slots.size() - lv_off.back()));
+    }
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    orb_status st = ensure_level_buffers(ctx, n_total, max_cells, (uint32_t)heap_cells);
+    if (st != ORB_OK) return st;
+    ORB_CUDA(ctx->idx.ensure(n_total + 1));
+    ORB_CUDA(ctx->batch_roots.ensure(k + 1));
+    ORB_CUDA(ctx->batch_slots.ensure(slots.size() + 1));
+    cudaStream_t s = ctx->stream;
+    float *dx = x, *dy = y, *dz = z;
+    float h2d_ms = 0.f, d2h_ms = 0.f;
+    if (!dev) {
+        ORB_CUDA(ctx->x.ensure(n_total + 1));
+        ORB_CUDA(ctx->y.ensure(n_total + 1));
+        ORB_CUDA(ctx->z.ensure(n_total + 1));
+        dx = ctx->x.p;
+        dy = ctx->y.p;
+        dz = ctx->z.p;
+        ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
+        if (n_total) {
+            ORB_CUDA(cudaMemcpyAsync(dx, x, n_total * sizeof(float), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaMemcpyAsync(dy, y, n_total * sizeof(float), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaMemcpyAsync(dz, z, n_total * sizeof(float), cudaMemcpyHostToDevice, s));
+        }
+        ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+    }
+    if (k) ORB_CUDA(cudaMemcpyAsync(ctx->batch_roots.p, roots.data(), k * sizeof(BatchRoot), cudaMemcpyHostToDevice, s));
+    if (!slots.empty())
+        ORB_CUDA(cudaMemcpyAsync(ctx->batch_slots.p, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
+    ORB_CUDA(cudaMemsetAsync(ctx->heap.p, 0, heap_cells * sizeof(orb_cell_t), s));
+    ORB_CUDA(cudaMemsetAsync(ctx->ranges.p, 0, heap_cells * sizeof(uint2), s));
+    ORB_CUDA(cudaMemsetAsync(ctx->counters.p, 0, sizeof(BuildCounters), s));
+    Level v = make_level(ctx, dx, dy, dz);
+    ctx->launches[kKInit] += 1;
+    launch_init_batch(v, ctx->batch_roots.p, (int)k, n_total, s);
+    ORB_CUDA(cudaGetLastError());
+    for (uint32_t l = 1; l <= max_levels; ++l) {
+        const size_t a = lv_off[l - 1], b = l < max_levels ? lv_off[l] : slots.size();
+        lv.push_back({0, ctx->batch_slots.p + a, (int)(b - a)});
+    }
+    uint32_t passes = 0;
+    st = run_levels(ctx, v, lv, &passes);
+    if (st != ORB_OK) return st;
+    ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    if (!dev) {
+        ORB_CUDA(cudaStreamSynchronize(s));
+        ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
+        ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
+        if (n_total) {
+            ORB_CUDA(cudaMemcpyAsync(x, dx, n_total * sizeof(float), cudaMemcpyDeviceToHost, s));
+            ORB_CUDA(cudaMemcpyAsync(y, dy, n_total * sizeof(float), cudaMemcpyDeviceToHost, s));
+            ORB_CUDA(cudaMemcpyAsync(z, dz, n_total * sizeof(float), cudaMemcpyDeviceToHost, s));
+        }
+    }
+    if (perm && n_total)
+        ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n_total * sizeof(uint32_t),
+                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (heap_cells) {
+        ORB_CUDA(cudaMemcpyAsync(heaps, ctx->heap.p, heap_cells * sizeof(orb_cell_t), cudaMemcpyDeviceToHost, s));
+        ORB_CUDA(cudaMemcpyAsync(ranges, ctx->ranges.p, heap_cells * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    }
+    ORB_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, sizeof(BuildCounters), cudaMemcpyDeviceToHost, s));
+    if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+    ORB_CUDA(cudaStreamSynchronize(s));
+    if (ctx->h_counters->error)
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
+    // ranges relative to each instance (cells the build filled)
+    for (uint32_t i = 0; i < k; ++i) {
+        const uint64_t filled = (2ull << lev[i]) - 1;
+        uint32_t *r = ranges + 2ull * roots[i].heap_base;
+        for (uint64_t j = 0; j < 2 * filled; ++j) r[j] -= roots[i].offset;
+    }
+    float dev_ms = 0.f;
+    ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
+    collect_profile(ctx);
+    for (int kk = 0; kk < kNumKernels; ++kk) ctx->prof_bytes[kk] += (double)ctx->h_counters->bytes[kk];
+    if (!dev) ORB_CUDA(cudaEventElapsedTime(&d2h_ms, ctx->ev[2], ctx->ev[3]));
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->levels_built = max_levels;
+        info->degenerate_cells = ctx->h_counters->degenerate;
+        info->zero_volume_cells = ctx->h_counters->zero_volume;
+        info->unfound_cells = ctx->h_counters->unfound;
+        info->max_iterations = ctx->h_counters->max_iters;
+        info->count_passes = passes;
+        info->device_ms = dev_ms;
+        info->h2d_ms = h2d_ms;
+        info->d2h_ms = d2h_ms;
+    }
     return ORB_OK;
 }
 

@@ -18,7 +18,8 @@ constexpr int kPWords = kPTile / 32; // bitmask words per partition tile
 constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
 constexpr int kThreads = 256;
 
-enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2 };
+enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3 };
+constexpr int kWarpKeys = 1024;      // cells up to this size bisect in one warp's registers
 
 // Kernel kinds, for launch counting, event timing and algorithmic-byte accounting.
 enum Kernel : int {
@@ -36,6 +37,7 @@ enum Kernel : int {
     kKEdges,
     kKBisectCta,
     kKTileMap,
+    kKBisectWarp,
     kNumKernels
 };
 extern const char *const kKernelNames[kNumKernels];
@@ -117,10 +119,21 @@ __device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {
     return axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
 }
 
+// Root of one instance of a batched build.
+struct BatchRoot {
+    uint32_t offset;     // first particle
+    uint32_t n;          // particles
+    uint32_t d;          // leaf cells
+    uint32_t heap_base;  // heap slot of the root
+    float lower[3], upper[3];
+};
+
 // Host-side launchers (orb_kernels.cu). `grid` is the CTA count of the tile loops.
 void launch_init(const Level &v, uint64_t n, const float lower[3], const float upper[3],
                  uint32_t d, int heap_cells, cudaStream_t st);
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st);
+void launch_init_batch(const Level &v, const BatchRoot *roots, int k, uint64_t n_total,
+                       cudaStream_t st);
 cudaError_t configure_kernels();  // once per device (dynamic shared memory limits)
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);

@@ -24,7 +24,7 @@ namespace orb {
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_edges",
-    "bisect_cta", "tile_map"};
+    "bisect_cta", "tile_map", "bisect_warp"};
 
 namespace {
 
@@ -227,6 +227,35 @@ __global__ void k_init(Level v, uint32_t n, float lo0, float lo1, float lo2, flo
     }
 }
 
+// Batched init: every instance's root cell and root range (heap and ranges are zeroed by
+// the host before) and idx = position relative to the instance. blockIdx.y walks the
+// instances, blockIdx.x their particles.
+__global__ void k_init_batch(Level v, const BatchRoot *roots, int k) {
+    for (int i = blockIdx.y; i < k; i += gridDim.y) {
+        const BatchRoot r = roots[i];
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            orb_cell_t c;
+            c.id = 0;
+            c.nLeafCells = (int32_t)r.d;
+            c.prevCutAxis = -1;
+            c.cutAxis = 0;  // orbit.cpp:75
+            c.foundCut = 0;
+            c.pad_[0] = c.pad_[1] = c.pad_[2] = 0;
+            for (int a = 0; a < 3; ++a) {
+                c.lower[a] = r.lower[a];
+                c.upper[a] = r.upper[a];
+            }
+            c.cutMarginLeft = r.lower[0];  // setCutMargin, orbit.cpp:76
+            c.cutMarginRight = r.upper[0];
+            v.heap[r.heap_base] = c;
+            v.ranges[r.heap_base] = make_uint2(r.offset, r.offset + r.n);
+        }
+        if (v.idx)
+            for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < r.n; p += gridDim.x * blockDim.x)
+                v.idx[r.offset + p] = p;
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // Plan: per-cell tile and histogram offsets (single CTA, any C).
 // ------------------------------------------------------------------------------------
@@ -255,7 +284,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
         v.ptile_off[c] = pp;
         pp += (n + kPTile - 1) / kPTile;
         v.hist_k[c] = (uint8_t)k;
-        v.state[c] = kActive;
+        v.state[c] = n <= (uint32_t)kWarpKeys ? kSmall : kActive;
         v.iters[c] = 0;
         v.below[c] = 0;
         v.inb[c] = n;
@@ -301,7 +330,7 @@ __device__ __forceinline__ float *cell_edges(const Level &v, int c) {
 // Edge tables of every cell for the first histogram pass of a level (warp per cell).
 __global__ void __launch_bounds__(kThreads) k_edges(Level v) {
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (c >= v.C) return;
+    if (c >= v.C || v.state[c] != kActive) return;
     const orb_cell_t &cell = v.heap[level_slot(v, c)];
     warp_edges(cell_edges(v, c), cell.cutMarginLeft, cell.cutMarginRight, v.hist_k[c]);
 }
@@ -481,6 +510,62 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         atomicMax(&v.counters->max_iters, it);
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
         if (st == kActive) v.counters->any_active = 1u;
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Bisection of small cells (at most kWarpKeys keys): one warp per cell, the keys held in
+// registers, every iteration of the reference loop (src/orbit.cpp:146-232) a register
+// count plus a warp reduction. Cells of other sizes are left to the histogram passes.
+// ------------------------------------------------------------------------------------
+constexpr int kWarpKeysPerLane = kWarpKeys / 32;
+
+__global__ void __launch_bounds__(kThreads) k_bisect_warp(Level v) {
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= v.C || v.state[c] != kSmall) return;
+    const int slot = level_slot(v, c);
+    orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    float k[kWarpKeysPerLane];
+#pragma unroll
+    for (int j = 0; j < kWarpKeysPerLane; ++j) {
+        const uint32_t i = (uint32_t)(j * 32 + lane);
+        k[j] = i < n ? __ldg(keys + rg.x + i) : __int_as_float(0x7fc00000);  // NaN: never below
+    }
+    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    uint32_t it = 0;
+    uint8_t st = kActive;
+    while (st == kActive) {
+        if (it >= (uint32_t)kMaxIterations) {
+            st = kCapped;
+            break;
+        }
+        const float cut = mid_cut(L, R);
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
+        cnt = warp_sum(cnt);
+        ++it;
+        const int dir = convergence(cnt, n);
+        if (dir == 0)
+            st = kFound;
+        else if (dir > 0)
+            R = cut;
+        else
+            L = cut;
+    }
+    if (lane == 0) {
+        cell.cutMarginLeft = L;
+        cell.cutMarginRight = R;
+        cell.foundCut = st == kFound ? 1 : 0;
+        v.iters[c] = (uint8_t)it;
+        v.state[c] = st;
+        atomicMax(&v.counters->max_iters, it);
+        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+        add_bytes(v, kKBisectWarp, 4ull * n);
     }
 }
 
@@ -1258,6 +1343,12 @@ inline int grid_for(uint64_t n, int threads, int cap) {
 // ------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------
+void launch_init_batch(const Level &v, const BatchRoot *roots, int k, uint64_t n_total,
+                       cudaStream_t st) {
+    (void)n_total;
+    if (k > 0) k_init_batch<<<dim3(64, (unsigned)(k < 65535 ? k : 65535)), 256, 0, st>>>(v, roots, k);
+}
+
 void launch_init(const Level &v, uint64_t n, const float lower[3], const float upper[3],
                  uint32_t d, int heap_cells, cudaStream_t st) {
     uint64_t work = n > (uint64_t)heap_cells * 13 ? n : (uint64_t)heap_cells * 13;
@@ -1274,6 +1365,9 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;
         case kKTileMap: k_tile_map<<<grid, kThreads, 0, st>>>(v); break;
+        case kKBisectWarp:
+            k_bisect_warp<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
+            break;
         case kKEdges:
             k_edges<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;

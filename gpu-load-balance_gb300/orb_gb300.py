@@ -62,7 +62,7 @@ EXPORTS = [
     "orb_abi_version", "orb_status_string", "orb_last_error", "orb_ctx_create",
     "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
     "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
-    "orb_profile_reset", "orb_profile_read", "orb_count_left_static",
+    "orb_profile_reset", "orb_profile_read", "orb_count_left_static", "orb_build_batch",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -134,6 +134,12 @@ class BuildInfo(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchInstance(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_uint64), ("n", ctypes.c_uint64), ("d", ctypes.c_uint32),
+                ("levels", ctypes.c_uint32), ("lower", ctypes.c_float * 3),
+                ("upper", ctypes.c_float * 3)]
+
+
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64),
                 ("total_ms", ctypes.c_double), ("bytes", ctypes.c_double)]
@@ -190,6 +196,9 @@ def load(path: str = LIB_PATH):
     L.orb_profile_reset.argtypes = [vp, ctypes.c_int]
     L.orb_profile_read.restype = ctypes.c_int
     L.orb_profile_read.argtypes = [vp, ctypes.POINTER(KernelStat), ctypes.c_int]
+    L.orb_build_batch.restype = ctypes.c_int
+    L.orb_build_batch.argtypes = [vp, vp, vp, vp, u64, ctypes.POINTER(BatchInstance), u32, vp, vp,
+                                  vp, u32, ctypes.POINTER(BuildInfo)]
     L.orb_count_left_static.restype = ctypes.c_int
     L.orb_count_left_static.argtypes = [vp, vp, vp, u64, vp, u32, vp, u32, vp, vp]
     _lib = L
@@ -273,6 +282,41 @@ class Context:
                                 ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
         self._check(st)
         return BuildResult(heap, ranges, perm, info.as_dict())
+
+    def build_batch(self, x, y, z, instances, perm=True, device_pointers: bool = False):
+        """Batched build. `instances`: list of dicts {offset, n, d, levels=0, lower, upper}.
+        Returns (list of per-instance (heap, ranges) views, perm, info)."""
+        k = len(instances)
+        arr = (BatchInstance * max(k, 1))()
+        heap_cells = 0
+        bases = []
+        for i, ins in enumerate(instances):
+            b = arr[i]
+            b.offset = int(ins["offset"])
+            b.n = int(ins["n"])
+            b.d = int(ins["d"])
+            b.levels = int(ins.get("levels", 0))
+            for a in range(3):
+                b.lower[a] = ins.get("lower", (-0.5, -0.5, -0.5))[a]
+                b.upper[a] = ins.get("upper", (0.5, 0.5, 0.5))[a]
+            bases.append(heap_cells)
+            heap_cells += 2 * b.d - 1
+        n_total = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        heaps = np.zeros(max(heap_cells, 1), CELL_DTYPE)
+        ranges = np.zeros((max(heap_cells, 1), 2), np.uint32)
+        if perm is True:
+            perm = np.empty(n_total, np.uint32)
+        info = BuildInfo()
+        st = self.lib.orb_build_batch(self.h, _ptr(x), _ptr(y), _ptr(z), n_total, arr, k,
+                                      heaps.ctypes.data, ranges.ctypes.data, _ptr(perm),
+                                      ORB_DEVICE_POINTERS if device_pointers else 0,
+                                      ctypes.byref(info))
+        self._check(st)
+        parts = []
+        for i, ins in enumerate(instances):
+            hc = 2 * int(ins["d"]) - 1
+            parts.append((heaps[bases[i]:bases[i] + hc], ranges[bases[i]:bases[i] + hc]))
+        return parts, perm, info.as_dict()
 
     def generate(self, kind: int, seed: int, n: int, x, y, z, device_pointers: bool = False):
         self._check(self.lib.orb_generate(self.h, kind, seed, n, _ptr(x), _ptr(y), _ptr(z),

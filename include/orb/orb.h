@@ -116,6 +116,33 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
                      orb_build_info *info);
 
 /*
+ * Batched build (no counterpart in the reference, which builds one tree per run): k
+ * independent ORB instances of uneven sizes, packed in one set of particle arrays, built
+ * together level by level (every level's kernels cover the cells of all instances).
+ * Each instance's result is bit-identical to orb_build on that instance alone.
+ *   x, y, z    n_total packed coordinates; instance i owns [offset_i, offset_i + n_i)
+ *              (instances may not overlap); partitioned in place
+ *   inst       k instance descriptors
+ *   heaps      out: the instances' heaps back to back, instance i at sum_{j<i}(2 d_j - 1)
+ *   ranges     out: 2 uint32 per heap cell, relative to the instance's offset
+ *   perm       out, optional: per position, the original index within its instance
+ *   flags      ORB_DEVICE_POINTERS for device x,y,z,perm (heaps/ranges stay host)
+ */
+typedef struct orb_batch_instance {
+    uint64_t offset;
+    uint64_t n;
+    uint32_t d;      /* leaf cells, a power of two */
+    uint32_t levels; /* 0 = log2(d) */
+    float lower[3];
+    float upper[3];
+} orb_batch_instance;
+
+orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                           const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
+                           uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                           orb_build_info *info);
+
+/*
  * Service layer: the reference's per-rank services over particles resident in the context.
  * orb_load_particles copies n particles in (host or device per flags), sets the range map
  * to root = [0, n) and sizes it for cell ids below max_cells.
