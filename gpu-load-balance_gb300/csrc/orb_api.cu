@@ -89,7 +89,8 @@ struct orb_ctx {
     uint32_t loaded_cells = 0;
 
     // profiling: launch counts always; CUDA-event durations when `prof_timing` is set
-    bool prof_timing = false;
+    uint32_t prof_mask = 0;  // kernel kinds whose launches are event-timed
+    bool capturing = false;  // inside a graph capture
     uint64_t launches[kNumKernels] = {};
     double prof_ms[kNumKernels] = {};
     double prof_bytes[kNumKernels] = {};
@@ -99,6 +100,18 @@ struct orb_ctx {
     };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> ev_pool;
+
+    // CUDA graph of the last build's device work, replayed while the configuration matches
+    bool use_graphs = true;
+    struct Graph {
+        bool valid = false;
+        std::vector<uint64_t> key;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<Rec> recs;  // event pairs recorded inside the graph (profiling)
+        uint64_t launches[kNumKernels] = {};
+        uint32_t passes = 0;
+    } graph;
 };
 
 namespace {
@@ -221,14 +234,17 @@ cudaEvent_t take_event(orb_ctx *ctx) {
 void run_kernel(orb_ctx *ctx, Kernel k, const Level &v, int grid, int arg = 0) {
     ctx->launches[k] += 1;
     cudaEvent_t a = nullptr, b = nullptr;
-    if (ctx->prof_timing) {
+    if (ctx->prof_mask & (1u << k)) {
         a = take_event(ctx);
         b = take_event(ctx);
     }
-    if (a && b) cudaEventRecord(a, ctx->stream);
+    // Inside a stream capture the records are external, so they become event nodes of the
+    // graph and every replay times the kernel again.
+    const unsigned rf = ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (a && b) cudaEventRecordWithFlags(a, ctx->stream, rf);
     launch_level_kernel(k, v, grid, arg, ctx->stream);
     if (a && b) {
-        cudaEventRecord(b, ctx->stream);
+        cudaEventRecordWithFlags(b, ctx->stream, rf);
         ctx->recs.push_back({(int)k, a, b});
     }
 }
@@ -245,6 +261,98 @@ void collect_profile(orb_ctx *ctx) {
     cudaGetLastError();
 }
 
+void drop_graph(orb_ctx *ctx) {
+    orb_ctx::Graph &g = ctx->graph;
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+    for (auto &r : g.recs) {
+        ctx->ev_pool.push_back(r.a);
+        ctx->ev_pool.push_back(r.b);
+    }
+    g = orb_ctx::Graph();
+}
+
+// Adds the event durations of the graph's last replay to the per-kernel totals.
+void collect_graph_profile(orb_ctx *ctx) {
+    for (auto &r : ctx->graph.recs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.kind] += ms;
+    }
+    cudaGetLastError();
+}
+
+// Runs `body` (device work only, no host synchronisation) on the context stream, through a
+// CUDA graph keyed by `key`: captured on first use, replayed while the key stays the same.
+template <class Body>
+orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t *passes, Body &&body) {
+    cudaStream_t s = ctx->stream;
+    if (!ctx->use_graphs) return body(passes);
+    orb_ctx::Graph &g = ctx->graph;
+    if (!(g.valid && g.key == key)) {
+        drop_graph(ctx);
+        uint64_t before[kNumKernels];
+        std::memcpy(before, ctx->launches, sizeof before);
+        collect_profile(ctx);  // keep pending records out of the graph's list
+        ORB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        ctx->capturing = true;
+        uint32_t p = 0;
+        orb_status st = body(&p);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        ctx->capturing = false;
+        if (st != ORB_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            for (auto &r : ctx->recs) {
+                ctx->ev_pool.push_back(r.a);
+                ctx->ev_pool.push_back(r.b);
+            }
+            ctx->recs.clear();
+            cudaGetLastError();
+            return st != ORB_OK ? st : cuda_fail(ctx, e, "cudaStreamEndCapture");
+        }
+        g.graph = graph;
+        ORB_CUDA(cudaGraphInstantiate(&g.exec, graph, 0));
+        g.recs.swap(ctx->recs);
+        for (int k = 0; k < kNumKernels; ++k) {
+            g.launches[k] = ctx->launches[k] - before[k];
+            ctx->launches[k] = before[k];
+        }
+        g.passes = p;
+        g.key = key;
+        g.valid = true;
+    }
+    ORB_CUDA(cudaGraphLaunch(g.exec, s));
+    for (int k = 0; k < kNumKernels; ++k) ctx->launches[k] += g.launches[k];
+    *passes += g.passes;
+    return ORB_OK;
+}
+
+// Key of the device work of a build: sizes, box, every buffer address the kernels use.
+void key_add(std::vector<uint64_t> &key, const void *p) { key.push_back((uint64_t)(uintptr_t)p); }
+void key_add_f(std::vector<uint64_t> &key, float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, sizeof u);
+    key.push_back(u);
+}
+std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
+    std::vector<uint64_t> key;
+    for (const void *p : {(const void *)v.x, (const void *)v.y, (const void *)v.z, (const void *)v.idx,
+                          (const void *)v.heap, (const void *)v.ranges, (const void *)v.tile_off,
+                          (const void *)v.hist_off, (const void *)v.hist_k, (const void *)v.state,
+                          (const void *)v.iters, (const void *)v.hist, (const void *)v.below,
+                          (const void *)v.inb, (const void *)v.edges, (const void *)v.htile_cell,
+                          (const void *)v.ptile_cell, (const void *)v.ptile_off, (const void *)v.ge_bits,
+                          (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
+                          (const void *)v.pt_ge_pre, (const void *)v.pt_le_pre, (const void *)v.pt_status,
+                          (const void *)v.part_s, (const void *)v.part_i, (const void *)v.part_le,
+                          (const void *)v.counters})
+        key_add(key, p);
+    key.push_back((uint64_t)ctx->pt_status.cap);
+    key.push_back(ctx->prof_mask);
+    key.push_back((uint64_t)ctx->cta_min_cells);
+    return key;
+}
+
 void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     const int g = pass_grid(ctx);
     // look-back state of the tile scan: status words cleared, ticket at zero
@@ -257,20 +365,17 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
 }
 
-// Bisection of every cell of the level to completion (found or capped).
-orb_status run_bisection(orb_ctx *ctx, const Level &v, uint32_t *passes) {
-    for (int pass = 0;; ++pass) {
-        if (pass > 64) return fail(ctx, ORB_ERR_TIMEOUT, "bisection did not finish in 64 passes");
-        ORB_CUDA(cudaMemsetAsync(&ctx->counters.p->any_active, 0, sizeof(uint32_t), ctx->stream));
+// Bisection of every cell of the level to completion (found or capped): a fixed number of
+// histogram/resolve passes, with no host round trip (a pass after the level is done exits
+// at once on the device).
+orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes) {
+    for (int pass = 0; pass < kHistPasses; ++pass) {
+        v.pass = pass;
         run_kernel(ctx, kKHist, v, pass_grid(ctx));
         run_kernel(ctx, kKResolve, v, pass_grid(ctx));
-        ORB_CUDA(cudaGetLastError());
-        ORB_CUDA(cudaMemcpyAsync(&ctx->h_counters->any_active, &ctx->counters.p->any_active,
-                                 sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-        ORB_CUDA(cudaStreamSynchronize(ctx->stream));
         ++*passes;
-        if (!ctx->h_counters->any_active) break;
     }
+    ORB_CUDA(cudaGetLastError());
     return ORB_OK;
 }
 
@@ -362,6 +467,8 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             // Measured on GB300 (2^27 particles, 2^16 leaves): the multi-CTA histogram passes
             // beat one-CTA-per-cell at every level, so the CTA path is opt-in.
             ctx->cta_min_cells = env ? std::atoi(env) : 1 << 30;
+            const char *ng = std::getenv("ORB_NO_GRAPHS");
+            ctx->use_graphs = !(ng && ng[0] && ng[0] != '0');
         }
         if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess) {
             st = cuda_fail(ctx, e, "cudaMallocHost");
@@ -403,6 +510,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->batch_roots.release(); ctx->batch_slots.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
+    drop_graph(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -458,14 +566,25 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     }
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
-    ctx->launches[kKInit] += 1;
-    launch_init(v, n, lower, upper, d, (int)heap_cells, s);
-    ORB_CUDA(cudaGetLastError());
-    uint32_t passes = 0;
     std::vector<LevelDesc> lv;
     for (uint32_t l = 1; l <= levels; ++l)
         lv.push_back({(1 << (l - 1)) - 1, nullptr, 1 << (l - 1)});  // src/orbit.cpp:104-107
-    st = run_levels(ctx, v, lv, &passes);
+    std::vector<uint64_t> key = level_key(ctx, v);
+    key.push_back(0xB111D);  // single build
+    key.push_back(n);
+    key.push_back(d);
+    key.push_back(levels);
+    for (int a = 0; a < 3; ++a) {
+        key_add_f(key, lower[a]);
+        key_add_f(key, upper[a]);
+    }
+    uint32_t passes = 0;
+    st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
+        ctx->launches[kKInit] += 1;
+        launch_init(v, n, lower, upper, d, (int)heap_cells, s);
+        ORB_CUDA(cudaGetLastError());
+        return run_levels(ctx, v, lv, pp);
+    });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (!dev) {
@@ -487,10 +606,11 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
     ORB_CUDA(cudaStreamSynchronize(s));
     if (ctx->h_counters->error)
-        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up or a bisection did not finish");
     float dev_ms = 0.f;
     ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
     collect_profile(ctx);
+    if (ctx->use_graphs) collect_graph_profile(ctx);
     for (int k = 0; k < kNumKernels; ++k) ctx->prof_bytes[k] += (double)ctx->h_counters->bytes[k];
     if (!dev) ORB_CUDA(cudaEventElapsedTime(&d2h_ms, ctx->ev[2], ctx->ev[3]));
     if (info) {
@@ -733,7 +853,7 @@ orb_status orb_partition(orb_ctx *ctx, const orb_cell_t *cells, uint32_t n_cells
     ORB_CUDA(cudaStreamSynchronize(s));
     collect_profile(ctx);
     if (ctx->h_counters->error)
-        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up or a bisection did not finish");
     return ORB_OK;
 }
 
@@ -853,19 +973,35 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
     if (!slots.empty())
         ORB_CUDA(cudaMemcpyAsync(ctx->batch_slots.p, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
-    ORB_CUDA(cudaMemsetAsync(ctx->heap.p, 0, heap_cells * sizeof(orb_cell_t), s));
-    ORB_CUDA(cudaMemsetAsync(ctx->ranges.p, 0, heap_cells * sizeof(uint2), s));
-    ORB_CUDA(cudaMemsetAsync(ctx->counters.p, 0, sizeof(BuildCounters), s));
     Level v = make_level(ctx, dx, dy, dz);
-    ctx->launches[kKInit] += 1;
-    launch_init_batch(v, ctx->batch_roots.p, (int)k, n_total, s);
-    ORB_CUDA(cudaGetLastError());
     for (uint32_t l = 1; l <= max_levels; ++l) {
         const size_t a = lv_off[l - 1], b = l < max_levels ? lv_off[l] : slots.size();
         lv.push_back({0, ctx->batch_slots.p + a, (int)(b - a)});
     }
+    std::vector<uint64_t> key = level_key(ctx, v);
+    key.push_back(0xBA7C4);  // batched build
+    key.push_back(n_total);
+    key_add(key, ctx->batch_roots.p);
+    key_add(key, ctx->batch_slots.p);
+    for (uint32_t i = 0; i < k; ++i) {
+        key.push_back(inst[i].offset);
+        key.push_back(inst[i].n);
+        key.push_back(((uint64_t)inst[i].d << 32) | lev[i]);
+        for (int a = 0; a < 3; ++a) {
+            key_add_f(key, inst[i].lower[a]);
+            key_add_f(key, inst[i].upper[a]);
+        }
+    }
     uint32_t passes = 0;
-    st = run_levels(ctx, v, lv, &passes);
+    st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
+        ORB_CUDA(cudaMemsetAsync(ctx->heap.p, 0, heap_cells * sizeof(orb_cell_t), s));
+        ORB_CUDA(cudaMemsetAsync(ctx->ranges.p, 0, heap_cells * sizeof(uint2), s));
+        ORB_CUDA(cudaMemsetAsync(ctx->counters.p, 0, sizeof(BuildCounters), s));
+        ctx->launches[kKInit] += 1;
+        launch_init_batch(v, ctx->batch_roots.p, (int)k, n_total, s);
+        ORB_CUDA(cudaGetLastError());
+        return run_levels(ctx, v, lv, pp);
+    });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
     if (!dev) {
@@ -889,7 +1025,7 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
     if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
     ORB_CUDA(cudaStreamSynchronize(s));
     if (ctx->h_counters->error)
-        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up (partition look-back)");
+        return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up or a bisection did not finish");
     // ranges relative to each instance (cells the build filled)
     for (uint32_t i = 0; i < k; ++i) {
         const uint64_t filled = (2ull << lev[i]) - 1;
@@ -899,6 +1035,7 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
     float dev_ms = 0.f;
     ORB_CUDA(cudaEventElapsedTime(&dev_ms, ctx->ev[0], ctx->ev[1]));
     collect_profile(ctx);
+    if (ctx->use_graphs) collect_graph_profile(ctx);
     for (int kk = 0; kk < kNumKernels; ++kk) ctx->prof_bytes[kk] += (double)ctx->h_counters->bytes[kk];
     if (!dev) ORB_CUDA(cudaEventElapsedTime(&d2h_ms, ctx->ev[2], ctx->ev[3]));
     if (info) {
@@ -919,7 +1056,7 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
 // ---------------------------------------------------------------------------------------
 // Profiling
 // ---------------------------------------------------------------------------------------
-orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing) {
+orb_status orb_profile_reset(orb_ctx *ctx, uint32_t timing_mask) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -929,8 +1066,15 @@ orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing) {
         ctx->prof_ms[k] = 0.0;
         ctx->prof_bytes[k] = 0.0;
     }
-    ctx->prof_timing = enable_timing != 0;
+    ctx->prof_mask = timing_mask;
     return ORB_OK;
+}
+
+int orb_profile_kernel_index(const char *name) {
+    if (!name) return -1;
+    for (int k = 0; k < kNumKernels; ++k)
+        if (std::strcmp(name, kKernelNames[k]) == 0) return k;
+    return -1;
 }
 
 int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries) {

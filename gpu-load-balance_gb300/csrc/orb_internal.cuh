@@ -16,6 +16,9 @@ constexpr int kTile = 16384;         // keys per tile of the count-left passes
 constexpr int kPTile = 4096;         // positions per tile of the partition passes
 constexpr int kPWords = kPTile / 32; // bitmask words per partition tile
 constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
+// Histogram passes per level. Cells of more than kWarpKeys keys use trees of depth >= 9
+// (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
+constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
 
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3 };
@@ -48,10 +51,9 @@ struct BuildCounters {
     uint32_t zero_volume;
     uint32_t unfound;
     uint32_t max_iters;
-    uint32_t any_active;  // set by the resolve step when a cell still needs a pass
+    uint32_t any_active[2];  // pass p: cleared by hist p, set by resolve p if a cell goes on
     uint32_t error;       // set when a bounded device wait gave up
     uint32_t ticket;      // block ticket of the tile scan (reset before each launch)
-    uint32_t pad;
     unsigned long long bytes[16];  // algorithmic bytes per Kernel kind
 };
 
@@ -65,6 +67,7 @@ struct Level {
     const int *slots;       // optional explicit slot list [C]
     int base;
     int C;
+    int pass;               // histogram pass index within the level
     // plan
     uint32_t *tile_off;     // [C+1] first tile of each cell
     uint32_t *htile_cell;   // [tiles] cell of each count-left tile (null: binary search)

@@ -370,6 +370,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
     __shared__ uint32_t s_hist[1 << kMaxBinsLog2];
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
+    if (blockIdx.x == 0 && threadIdx.x == 0) v.counters->any_active[v.pass & 1] = 0u;
+    // every cell of the level finished in an earlier pass: nothing to bin
+    if (v.pass > 0 && *(volatile uint32_t *)&v.counters->any_active[(v.pass - 1) & 1] == 0u) return;
     const uint32_t total = v.tile_off[v.C];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const TileRef tr = tile_ref(v, t);
@@ -509,7 +512,11 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         v.below[c] = 0;
         atomicMax(&v.counters->max_iters, it);
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
-        if (st == kActive) v.counters->any_active = 1u;
+        if (st == kActive) {
+            v.counters->any_active[v.pass & 1] = 1u;
+            // the last pass leaves no cell active (tree depths >= 9): flag it if one does
+            if (v.pass == kHistPasses - 1) atomicExch(&v.counters->error, 1u);
+        }
     }
 }
 

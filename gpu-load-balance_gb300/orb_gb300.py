@@ -63,6 +63,7 @@ EXPORTS = [
     "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
     "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
     "orb_profile_reset", "orb_profile_read", "orb_count_left_static", "orb_build_batch",
+    "orb_profile_kernel_index",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -193,7 +194,9 @@ def load(path: str = LIB_PATH):
     L.orb_generate.restype = ctypes.c_int
     L.orb_generate.argtypes = [vp, ctypes.c_int, u64, u64, vp, vp, vp, u32]
     L.orb_profile_reset.restype = ctypes.c_int
-    L.orb_profile_reset.argtypes = [vp, ctypes.c_int]
+    L.orb_profile_reset.argtypes = [vp, u32]
+    L.orb_profile_kernel_index.restype = ctypes.c_int
+    L.orb_profile_kernel_index.argtypes = [ctypes.c_char_p]
     L.orb_profile_read.restype = ctypes.c_int
     L.orb_profile_read.argtypes = [vp, ctypes.POINTER(KernelStat), ctypes.c_int]
     L.orb_build_batch.restype = ctypes.c_int
@@ -266,12 +269,14 @@ class Context:
             pass
 
     def build(self, x, y, z, d: int, levels: int = 0, lower=(-0.5, -0.5, -0.5),
-              upper=(0.5, 0.5, 0.5), perm=True, device_pointers: bool = False) -> BuildResult:
+              upper=(0.5, 0.5, 0.5), perm=True, device_pointers: bool = False,
+              heap_out=None, ranges_out=None) -> BuildResult:
         """ORB build. Host numpy arrays are partitioned in place; with device_pointers the
-        arguments are device tensors/pointers partitioned in place on the device."""
+        arguments are device tensors/pointers partitioned in place on the device. heap_out /
+        ranges_out may supply (for instance pinned) host arrays for the results."""
         n = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
-        heap = np.zeros(2 * d - 1, CELL_DTYPE)
-        ranges = np.zeros((2 * d - 1, 2), np.uint32)
+        heap = np.zeros(2 * d - 1, CELL_DTYPE) if heap_out is None else heap_out
+        ranges = np.zeros((2 * d - 1, 2), np.uint32) if ranges_out is None else ranges_out
         if perm is True:
             perm = np.empty(n, np.uint32)
         lo = np.asarray(lower, np.float32)
@@ -328,8 +333,20 @@ class Context:
         return x, y, z
 
     # profiling -----------------------------------------------------------------------
-    def profile_reset(self, timing: bool = False):
-        self._check(self.lib.orb_profile_reset(self.h, 1 if timing else 0))
+    def profile_reset(self, timing=False):
+        """timing: False (counts only), True (time every kernel) or a list of kernel names."""
+        if timing is True:
+            mask = 0xFFFFFFFF
+        elif not timing:
+            mask = 0
+        else:
+            mask = 0
+            for name in timing:
+                k = self.lib.orb_profile_kernel_index(name.encode())
+                if k < 0:
+                    raise OrbError(1, f"unknown kernel {name}")
+                mask |= 1 << k
+        self._check(self.lib.orb_profile_reset(self.h, mask))
 
     def profile(self) -> dict:
         """{kernel name: {launches, total_ms, bytes}} since the last profile_reset."""

@@ -181,10 +181,11 @@ orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float
 
 /*
  * Per-kernel profile of a context (no reference counterpart; the reference prints phase
- * wall-clock timers, src/orbit.cpp:284-286). Launch counts are always kept; with
- * enable_timing, every launch is bracketed by CUDA events on the context stream and the
- * durations are summed. `bytes` is the algorithmic traffic those launches moved (keys read,
- * table entries written, particles swapped), counted on the device.
+ * wall-clock timers, src/orbit.cpp:284-286). Launch counts are always kept. Launches of the
+ * kernel kinds selected by timing_mask (bit orb_profile_kernel_index(name); 0xffffffff =
+ * all) are bracketed by CUDA events on the context stream and their durations summed.
+ * `bytes` is the algorithmic traffic those launches moved (keys read, masks written,
+ * particles swapped), counted on the device.
  */
 typedef struct orb_kernel_stat {
     char name[32];
@@ -192,7 +193,9 @@ typedef struct orb_kernel_stat {
     double total_ms;
     double bytes;
 } orb_kernel_stat;
-orb_status orb_profile_reset(orb_ctx *ctx, int enable_timing);
+orb_status orb_profile_reset(orb_ctx *ctx, uint32_t timing_mask);
+/* Index of a kernel kind by the name orb_profile_read reports, or -1. */
+int orb_profile_kernel_index(const char *name);
 /* Writes up to max_entries stats (kernels launched at least once); returns how many exist. */
 int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries);
 
