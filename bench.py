@@ -196,6 +196,76 @@ def reference_arm(args):
 
 
 # ------------------------------------------------------------------------------------------
+# Batched workload: 128 uneven instances, batched build vs one instance at a time
+# ------------------------------------------------------------------------------------------
+def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
+    import numpy as np
+    import workloads as W
+
+    specs = W.batched_instances(seed, 128)
+    offs, total = [], 0
+    for sp in specs:
+        offs.append(total)
+        total += sp.n
+    x0, y0, z0 = (torch.empty(total, dtype=torch.float32, device=dev) for _ in range(3))
+    for sp, off in zip(specs, offs):
+        kind = E.ORB_GEN_UNIFORM if sp.kind == "uniform" else E.ORB_GEN_PLUMMER
+        ctx.generate(kind, sp.seed, sp.n, x0[off:off + sp.n], y0[off:off + sp.n], z0[off:off + sp.n],
+                     device_pointers=True)
+    x, y, z = (torch.empty_like(x0) for _ in range(3))
+    perm = torch.empty(total, dtype=torch.int32, device=dev)
+    inst = [{"offset": off, "n": sp.n, "d": sp.d} for sp, off in zip(specs, offs)]
+    outs = [(np.zeros(2 * sp.d - 1, E.CELL_DTYPE), np.zeros((2 * sp.d - 1, 2), np.uint32))
+            for sp in specs]
+
+    def restore():
+        x.copy_(x0)
+        y.copy_(y0)
+        z.copy_(z0)
+        torch.cuda.synchronize(dev)
+
+    def batch_step():
+        restore()
+        return ctx.build_batch(x, y, z, inst, perm=perm, device_pointers=True)
+
+    def plain_step():
+        restore()
+        for sp, off, (hp, rp) in zip(specs, offs, outs):
+            sl = slice(off, off + sp.n)
+            ctx.build(x[sl], y[sl], z[sl], sp.d, perm=perm[sl], device_pointers=True,
+                      heap_out=hp, ranges_out=rp)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        for _ in range(steps):
+            r = fn()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t) / steps, r
+
+    ctx.profile_reset(timing=False)
+    t_batch, (parts, _, binfo) = timed(batch_step)
+    bperm = perm.cpu().numpy()
+    t_plain, _ = timed(plain_step)
+    pperm = perm.cpu().numpy()
+    same = all(hb.tobytes() == hp.tobytes() and np.array_equal(rb, rp)
+               for (hb, rb), (hp, rp) in zip(parts, outs)) and np.array_equal(bperm, pperm)
+    return {
+        "workload": "128 instances, particles log-uniform 2^14..2^22, leaves 2^6..2^12, "
+                    "half uniform / half Plummer (seeded)",
+        "particles": total, "instances": len(specs),
+        "instances_per_s": len(specs) / t_batch,
+        "plain_instances_per_s": len(specs) / t_plain,
+        "speedup_vs_plain": t_plain / t_batch,
+        "ms_per_batch": 1e3 * t_batch, "ms_plain_one_at_a_time": 1e3 * t_plain,
+        "particles_per_s": total / t_batch,
+        "bit_exact_vs_plain": bool(same),
+    }
+
+
+# ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
 def gpu_arm(args):
@@ -322,6 +392,10 @@ def gpu_arm(args):
                for k, v in warm.items()}
     launches = sum(v["launches"] for v in prof.values())
 
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched(ctx, E, torch, dev, max(2, min(args.steps, 5)), 1, SEED + 77)
+
     cpu = None
     if not args.no_cpu_baseline:
         cpu = run_cpu(1, 0, budget_s=40.0)
@@ -346,6 +420,7 @@ def gpu_arm(args):
         "kernels_per_step_warmup": kernels,
         "gpu_launches": launches,
         "cpu_baseline": cpu,
+        "batched": batched,
         "clocks": clocks.summary(tw0, te1),
         "bisection_passes_per_build": infos[-1]["count_passes"],
     }
@@ -365,6 +440,7 @@ def main():
     ap.add_argument("--particles", type=int, default=N_PARTICLES)
     ap.add_argument("--leaves", type=int, default=LEAVES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

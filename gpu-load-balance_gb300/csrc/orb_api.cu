@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <list>
 #include <mutex>
 #include <new>
 #include <string>
@@ -101,17 +102,20 @@ struct orb_ctx {
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> ev_pool;
 
-    // CUDA graph of the last build's device work, replayed while the configuration matches
+    // CUDA graphs of recent builds' device work (most recent first), replayed when the
+    // configuration matches
     bool use_graphs = true;
     struct Graph {
-        bool valid = false;
         std::vector<uint64_t> key;
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         std::vector<Rec> recs;  // event pairs recorded inside the graph (profiling)
         uint64_t launches[kNumKernels] = {};
         uint32_t passes = 0;
-    } graph;
+    };
+    std::list<Graph> graphs;
+    Graph *last_graph = nullptr;  // the graph of the last build (for its profile)
+    static constexpr size_t kMaxGraphs = 256;
 };
 
 namespace {
@@ -261,8 +265,7 @@ void collect_profile(orb_ctx *ctx) {
     cudaGetLastError();
 }
 
-void drop_graph(orb_ctx *ctx) {
-    orb_ctx::Graph &g = ctx->graph;
+void drop_graph(orb_ctx *ctx, orb_ctx::Graph &g) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     if (g.graph) cudaGraphDestroy(g.graph);
     for (auto &r : g.recs) {
@@ -272,9 +275,16 @@ void drop_graph(orb_ctx *ctx) {
     g = orb_ctx::Graph();
 }
 
-// Adds the event durations of the graph's last replay to the per-kernel totals.
+void drop_all_graphs(orb_ctx *ctx) {
+    for (auto &g : ctx->graphs) drop_graph(ctx, g);
+    ctx->graphs.clear();
+    ctx->last_graph = nullptr;
+}
+
+// Adds the event durations of the last replayed graph to the per-kernel totals.
 void collect_graph_profile(orb_ctx *ctx) {
-    for (auto &r : ctx->graph.recs) {
+    if (!ctx->last_graph) return;
+    for (auto &r : ctx->last_graph->recs) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.kind] += ms;
     }
@@ -286,10 +296,20 @@ void collect_graph_profile(orb_ctx *ctx) {
 template <class Body>
 orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t *passes, Body &&body) {
     cudaStream_t s = ctx->stream;
+    ctx->last_graph = nullptr;
     if (!ctx->use_graphs) return body(passes);
-    orb_ctx::Graph &g = ctx->graph;
-    if (!(g.valid && g.key == key)) {
-        drop_graph(ctx);
+    auto hit = ctx->graphs.begin();
+    for (; hit != ctx->graphs.end(); ++hit)
+        if (hit->key == key) break;
+    if (hit != ctx->graphs.end()) {
+        ctx->graphs.splice(ctx->graphs.begin(), ctx->graphs, hit);  // most recent first
+    } else {
+        if (ctx->graphs.size() >= orb_ctx::kMaxGraphs) {
+            drop_graph(ctx, ctx->graphs.back());
+            ctx->graphs.pop_back();
+        }
+        ctx->graphs.emplace_front();
+        orb_ctx::Graph &g = ctx->graphs.front();
         uint64_t before[kNumKernels];
         std::memcpy(before, ctx->launches, sizeof before);
         collect_profile(ctx);  // keep pending records out of the graph's list
@@ -307,11 +327,17 @@ orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t 
                 ctx->ev_pool.push_back(r.b);
             }
             ctx->recs.clear();
+            ctx->graphs.pop_front();
             cudaGetLastError();
             return st != ORB_OK ? st : cuda_fail(ctx, e, "cudaStreamEndCapture");
         }
         g.graph = graph;
-        ORB_CUDA(cudaGraphInstantiate(&g.exec, graph, 0));
+        cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (ie != cudaSuccess) {
+            drop_graph(ctx, g);
+            ctx->graphs.pop_front();
+            return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        }
         g.recs.swap(ctx->recs);
         for (int k = 0; k < kNumKernels; ++k) {
             g.launches[k] = ctx->launches[k] - before[k];
@@ -319,11 +345,12 @@ orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t 
         }
         g.passes = p;
         g.key = key;
-        g.valid = true;
     }
+    orb_ctx::Graph &g = ctx->graphs.front();
     ORB_CUDA(cudaGraphLaunch(g.exec, s));
     for (int k = 0; k < kNumKernels; ++k) ctx->launches[k] += g.launches[k];
     *passes += g.passes;
+    ctx->last_graph = &g;
     return ORB_OK;
 }
 
@@ -510,7 +537,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->batch_roots.release(); ctx->batch_slots.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
-    drop_graph(ctx);
+    drop_all_graphs(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
