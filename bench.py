@@ -266,6 +266,70 @@ def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
 
 
 # ------------------------------------------------------------------------------------------
+# Served workload: Poisson request stream, continuous batching vs one request at a time
+# ------------------------------------------------------------------------------------------
+def run_server_stream(E, device, reqs, budget, max_batch, lanes, paced=True):
+    """Submits `reqs` at their arrival times (or all at once when paced=False); returns the
+    per-request results and the server stats."""
+    with E.Server(device, hbm_budget_bytes=budget, max_batch=max_batch, lanes=lanes) as sv:
+        # warm-up: every lane allocates its build scratch once
+        warm = [sv.submit_generate(E.ORB_GEN_UNIFORM, 1, 1 << 16, 64) for _ in range(2 * lanes)]
+        for w in warm:
+            sv.wait(w)
+        for w in warm:
+            sv.release(w)
+        inst, rids = {}, []
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            delay = t0 + r.t - time.perf_counter()
+            if paced and delay > 0:
+                time.sleep(delay)
+            if r.kind == "build":
+                kind = E.ORB_GEN_UNIFORM if r.spec.kind == "uniform" else E.ORB_GEN_PLUMMER
+                rid = sv.submit_generate(kind, r.spec.seed, r.spec.n, r.spec.d)
+                inst[i] = rid
+            else:
+                rid = sv.submit_rebalance(inst[r.target], r.seed, 1e-3)
+            rids.append(rid)
+        res = [sv.wait(rid) for rid in rids]
+        stats = sv.stats()
+    return res, stats
+
+
+def bench_served(E, device, seed: int, rate: float = 2000.0, count: int = 2000):
+    import workloads as W
+
+    reqs = W.served_stream(seed, rate, count, rebalance_frac=0.5, sizes=(14, 22))
+    budget = 96 << 30
+
+    def summarize(res, stats):
+        lat = sorted(r["done_s"] - r["submit_s"] for r in res)
+        span = max(r["done_s"] for r in res) - min(r["submit_s"] for r in res)
+        ok = all(r["status"] == 0 for r in res)
+        return {"instances_per_s": len(res) / span, "p50_ms": 1e3 * lat[len(lat) // 2],
+                "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                "batches": stats["batches"], "mean_batch": len(res) / max(stats["batches"], 1),
+                "max_batch": stats["max_batch_seen"], "all_ok": ok}
+
+    cb = summarize(*run_server_stream(E, device, reqs, budget, 0, 2))
+    one = summarize(*run_server_stream(E, device, reqs, budget, 1, 1))
+    # capacity: the same requests submitted all at once
+    cb_sat = summarize(*run_server_stream(E, device, reqs, budget, 0, 2, paced=False))
+    one_sat = summarize(*run_server_stream(E, device, reqs, budget, 1, 1, paced=False))
+    return {
+        "workload": f"Poisson arrivals at {rate:.0f} req/s, {count} requests, half new instances "
+                    "(particles log-uniform 2^14..2^22, leaves 2^6..2^12, half uniform / half "
+                    "Plummer, generated on the device) and half rebalances (sigma=1e-3) of "
+                    "resident instances",
+        "paced": {"continuous_batching": cb, "one_at_a_time": one,
+                  "speedup_instances_per_s": cb["instances_per_s"] / one["instances_per_s"],
+                  "note": "continuous batching keeps up with the arrival rate, which caps it"},
+        "saturated": {"continuous_batching": cb_sat, "one_at_a_time": one_sat,
+                      "speedup_instances_per_s": cb_sat["instances_per_s"] / one_sat["instances_per_s"]},
+    }
+
+
+# ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
 def gpu_arm(args):
@@ -395,6 +459,11 @@ def gpu_arm(args):
     batched = None
     if not args.no_batched:
         batched = bench_batched(ctx, E, torch, dev, max(2, min(args.steps, 5)), 1, SEED + 77)
+    served = None
+    if not args.no_served:
+        del x0, y0, z0, x, y, z  # give the server's arena the memory
+        torch.cuda.empty_cache()
+        served = bench_served(E, local, SEED + 99)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -421,6 +490,7 @@ def gpu_arm(args):
         "gpu_launches": launches,
         "cpu_baseline": cpu,
         "batched": batched,
+        "served": served,
         "clocks": clocks.summary(tw0, te1),
         "bisection_passes_per_build": infos[-1]["count_passes"],
     }
@@ -441,6 +511,7 @@ def main():
     ap.add_argument("--leaves", type=int, default=LEAVES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -441,6 +441,14 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
 
 }  // namespace
 
+namespace orb {
+cudaStream_t ctx_stream(orb_ctx *ctx) { return ctx->stream; }
+void ctx_disable_graphs(orb_ctx *ctx) {
+    ctx->use_graphs = false;
+    drop_all_graphs(ctx);
+}
+}  // namespace orb
+
 extern "C" {
 
 int orb_abi_version(void) { return ORB_ABI_VERSION; }
@@ -1041,9 +1049,14 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
             ORB_CUDA(cudaMemcpyAsync(z, dz, n_total * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
     }
-    if (perm && n_total)
-        ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n_total * sizeof(uint32_t),
-                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (perm && n_total) {
+        if (dev) {  // only the instances' positions: the rest of `perm` is the caller's
+            launch_copy_instances(ctx->idx.p, perm, ctx->batch_roots.p, (int)k, s);
+            ORB_CUDA(cudaGetLastError());
+        } else {
+            ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n_total * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        }
+    }
     if (heap_cells) {
         ORB_CUDA(cudaMemcpyAsync(heaps, ctx->heap.p, heap_cells * sizeof(orb_cell_t), cudaMemcpyDeviceToHost, s));
         ORB_CUDA(cudaMemcpyAsync(ranges, ctx->ranges.p, heap_cells * sizeof(uint2), cudaMemcpyDeviceToHost, s));

@@ -137,10 +137,25 @@ void launch_init(const Level &v, uint64_t n, const float lower[3], const float u
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st);
 void launch_init_batch(const Level &v, const BatchRoot *roots, int k, uint64_t n_total,
                        cudaStream_t st);
+// dst[p] = src[p] for the positions of every instance (2-D grid: instance x particles)
+void launch_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *roots, int k,
+                           cudaStream_t st);
+// Gaussian displacement of the particles [offset, offset+n): x += sigma * N(0,1) per
+// coordinate, clamped to [lower, nextafter(upper, lower)] (seeded, counter-based)
+void launch_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n, uint64_t seed,
+                     float sigma, const float lower[3], const float upper[3], cudaStream_t st);
 cudaError_t configure_kernels();  // once per device (dynamic shared memory limits)
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);
 void launch_gen_plummer(uint64_t seed, uint64_t n, const float *centres, const double *scales,
                         float *x, float *y, float *z, cudaStream_t st);
+
+// Context internals used by the request server (orb_server.cu).
+cudaStream_t ctx_stream(orb_ctx *ctx);
+void ctx_disable_graphs(orb_ctx *ctx);
+void launch_iota_u32(uint32_t *dst, uint64_t n, cudaStream_t st);  // dst[p] = p
+// gather: dst[off+p] = src[off + perm[off+p]] for p < n (instance-relative permutation)
+void launch_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
+                       uint64_t n, cudaStream_t st);
 
 }  // namespace orb

@@ -1338,6 +1338,49 @@ __global__ void k_gen_plummer(uint64_t seed, uint64_t n, PlummerTable tab, float
     }
 }
 
+__global__ void k_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *roots, int k) {
+    for (int i = blockIdx.y; i < k; i += gridDim.y) {
+        const BatchRoot r = roots[i];
+        for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < r.n; p += gridDim.x * blockDim.x)
+            dst[r.offset + p] = src[r.offset + p];
+    }
+}
+
+// Box-Muller pairs from the counter-based stream: coordinate a of particle i uses draws
+// (seed, 2*(3i+a)) and (seed, 2*(3i+a)+1).
+__global__ void k_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n,
+                           uint64_t seed, float sigma, float lo0, float lo1, float lo2,
+                           float hi0, float hi1, float hi2) {
+    const uint64_t sm = mix64(seed);
+    float *c[3] = {x, y, z};
+    const float lo[3] = {lo0, lo1, lo2};
+    const float hi[3] = {nextafterf(hi0, lo0), nextafterf(hi1, lo1), nextafterf(hi2, lo2)};
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        for (int a = 0; a < 3; ++a) {
+            const uint64_t q = 2 * (3 * i + a);
+            const float u1 = ((float)(uint32_t)(draw(sm, q) >> 40) + 1.0f) * 0x1p-24f;  // (0, 1]
+            const float u2 = (float)(uint32_t)(draw(sm, q + 1) >> 40) * 0x1p-24f;       // [0, 1)
+            const float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+            const float p = c[a][offset + i] + sigma * g;
+            c[a][offset + i] = fminf(fmaxf(p, lo[a]), hi[a]);
+        }
+    }
+}
+
+__global__ void k_iota_u32(uint32_t *dst, uint64_t n) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (uint64_t)gridDim.x * blockDim.x)
+        dst[p] = (uint32_t)p;
+}
+
+__global__ void k_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
+                             uint64_t n) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (uint64_t)gridDim.x * blockDim.x)
+        dst[off + p] = src[off + perm[off + p]];
+}
+
 inline int grid_for(uint64_t n, int threads, int cap) {
     uint64_t g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -1398,6 +1441,29 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
 cudaError_t configure_kernels() {
     return cudaFuncSetAttribute(k_bisect_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kCtaSmemBytes);
+}
+
+void launch_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *roots, int k,
+                           cudaStream_t st) {
+    if (k > 0)
+        k_copy_instances<<<dim3(64, (unsigned)(k < 65535 ? k : 65535)), 256, 0, st>>>(src, dst, roots, k);
+}
+
+void launch_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n, uint64_t seed,
+                     float sigma, const float lower[3], const float upper[3], cudaStream_t st) {
+    if (n == 0) return;
+    k_displace<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(x, y, z, offset, n, seed, sigma, lower[0],
+                                                          lower[1], lower[2], upper[0], upper[1],
+                                                          upper[2]);
+}
+
+void launch_iota_u32(uint32_t *dst, uint64_t n, cudaStream_t st) {
+    if (n) k_iota_u32<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, n);
+}
+
+void launch_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
+                       uint64_t n, cudaStream_t st) {
+    if (n) k_gather_u32<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, perm, off, n);
 }
 
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,

@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liborb_gb300.so")
-SOURCES = ["orb_kernels.cu", "orb_api.cu", "orb_static.cu"]
+SOURCES = ["orb_kernels.cu", "orb_api.cu", "orb_static.cu", "orb_server.cu"]
 HEADERS = ["orb_internal.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -63,7 +63,9 @@ EXPORTS = [
     "orb_ctx_destroy", "orb_build", "orb_load_particles", "orb_store_particles", "orb_count",
     "orb_count_left", "orb_partition", "orb_get_ranges", "orb_set_ranges", "orb_generate",
     "orb_profile_reset", "orb_profile_read", "orb_count_left_static", "orb_build_batch",
-    "orb_profile_kernel_index",
+    "orb_profile_kernel_index", "orb_server_create", "orb_server_destroy", "orb_server_submit_build",
+    "orb_server_submit_generate", "orb_server_submit_rebalance", "orb_server_wait", "orb_server_poll",
+    "orb_server_fetch", "orb_server_release", "orb_server_get_stats",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -141,6 +143,28 @@ class BatchInstance(ctypes.Structure):
                 ("upper", ctypes.c_float * 3)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_uint32),
+                ("lanes", ctypes.c_uint32)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("instance_id", ctypes.c_uint64),
+                ("status", ctypes.c_int32), ("kind", ctypes.c_int32), ("batch_size", ctypes.c_uint32),
+                ("pad_", ctypes.c_uint32), ("submit_s", ctypes.c_double), ("start_s", ctypes.c_double),
+                ("done_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("requests_submitted", "requests_done", "builds",
+                                               "rebalances", "batches", "particles_built",
+                                               "arena_particles", "arena_used")] + \
+               [("max_batch_seen", ctypes.c_uint32), ("pending", ctypes.c_uint32)]
+
+
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_uint64),
                 ("total_ms", ctypes.c_double), ("bytes", ctypes.c_double)]
@@ -202,6 +226,26 @@ def load(path: str = LIB_PATH):
     L.orb_build_batch.restype = ctypes.c_int
     L.orb_build_batch.argtypes = [vp, vp, vp, vp, u64, ctypes.POINTER(BatchInstance), u32, vp, vp,
                                   vp, u32, ctypes.POINTER(BuildInfo)]
+    L.orb_server_create.restype = ctypes.c_int
+    L.orb_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
+    L.orb_server_destroy.restype = ctypes.c_int
+    L.orb_server_destroy.argtypes = [vp]
+    L.orb_server_submit_build.restype = ctypes.c_int
+    L.orb_server_submit_build.argtypes = [vp, vp, vp, vp, u64, u32, u32, vp, vp, ctypes.POINTER(u64)]
+    L.orb_server_submit_generate.restype = ctypes.c_int
+    L.orb_server_submit_generate.argtypes = [vp, ctypes.c_int, u64, u64, u32, u32, ctypes.POINTER(u64)]
+    L.orb_server_submit_rebalance.restype = ctypes.c_int
+    L.orb_server_submit_rebalance.argtypes = [vp, u64, u64, ctypes.c_float, ctypes.POINTER(u64)]
+    L.orb_server_wait.restype = ctypes.c_int
+    L.orb_server_wait.argtypes = [vp, u64, ctypes.POINTER(RequestResult)]
+    L.orb_server_poll.restype = ctypes.c_int
+    L.orb_server_poll.argtypes = [vp, ctypes.POINTER(RequestResult), u32, ctypes.POINTER(u32)]
+    L.orb_server_fetch.restype = ctypes.c_int
+    L.orb_server_fetch.argtypes = [vp, u64, vp, vp, vp, vp, vp, vp]
+    L.orb_server_release.restype = ctypes.c_int
+    L.orb_server_release.argtypes = [vp, u64]
+    L.orb_server_get_stats.restype = ctypes.c_int
+    L.orb_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
     L.orb_count_left_static.restype = ctypes.c_int
     L.orb_count_left_static.argtypes = [vp, vp, vp, u64, vp, u32, vp, u32, vp, vp]
     _lib = L
@@ -393,3 +437,83 @@ class Context:
     def set_ranges(self, ranges: np.ndarray):
         r = np.ascontiguousarray(ranges, np.uint32)
         self._check(self.lib.orb_set_ranges(self.h, r.ctypes.data, r.shape[0]))
+
+
+class Server:
+    """Continuous-batching ORB request server (orb_server_* of the C ABI)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 4 << 30, max_batch: int = 0,
+                 lanes: int = 2):
+        self.lib = load()
+        self.h = ctypes.c_void_p()
+        o = ServerOpts(hbm_budget_bytes, max_batch, lanes)
+        st = self.lib.orb_server_create(device, ctypes.byref(o), ctypes.byref(self.h))
+        if st != 0:
+            raise OrbError(st, "orb_server_create")
+        self.d = {}
+
+    def close(self):
+        if self.h:
+            self.lib.orb_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, st, what):
+        if st != 0:
+            raise OrbError(st, what)
+
+    def submit_build(self, x, y, z, d: int, levels: int = 0, lower=(-0.5, -0.5, -0.5),
+                     upper=(0.5, 0.5, 0.5)) -> int:
+        x, y, z = (np.ascontiguousarray(a, np.float32) for a in (x, y, z))
+        lo = np.asarray(lower, np.float32)
+        hi = np.asarray(upper, np.float32)
+        rid = ctypes.c_uint64()
+        self._chk(self.lib.orb_server_submit_build(self.h, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                                                   x.size, d, levels, lo.ctypes.data, hi.ctypes.data,
+                                                   ctypes.byref(rid)), "submit_build")
+        self.d[rid.value] = (d, x.size)
+        return rid.value
+
+    def submit_generate(self, kind: int, seed: int, n: int, d: int, levels: int = 0) -> int:
+        rid = ctypes.c_uint64()
+        self._chk(self.lib.orb_server_submit_generate(self.h, kind, seed, n, d, levels,
+                                                      ctypes.byref(rid)), "submit_generate")
+        self.d[rid.value] = (d, n)
+        return rid.value
+
+    def submit_rebalance(self, instance: int, seed: int, sigma: float) -> int:
+        rid = ctypes.c_uint64()
+        self._chk(self.lib.orb_server_submit_rebalance(self.h, instance, seed, sigma,
+                                                       ctypes.byref(rid)), "submit_rebalance")
+        return rid.value
+
+    def wait(self, request: int) -> dict:
+        r = RequestResult()
+        st = self.lib.orb_server_wait(self.h, request, ctypes.byref(r))
+        out = r.as_dict()
+        out["status"] = st
+        return out
+
+    def fetch(self, instance: int):
+        d, n = self.d[instance]
+        heap = np.zeros(2 * d - 1, CELL_DTYPE)
+        ranges = np.zeros((2 * d - 1, 2), np.uint32)
+        x, y, z = (np.empty(n, np.float32) for _ in range(3))
+        ident = np.empty(n, np.uint32)
+        self._chk(self.lib.orb_server_fetch(self.h, instance, heap.ctypes.data, ranges.ctypes.data,
+                                            x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                                            ident.ctypes.data), "fetch")
+        return heap, ranges, x, y, z, ident
+
+    def release(self, instance: int):
+        self._chk(self.lib.orb_server_release(self.h, instance), "release")
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self._chk(self.lib.orb_server_get_stats(self.h, ctypes.byref(s)), "stats")
+        return {k: getattr(s, k) for k, _ in s._fields_}

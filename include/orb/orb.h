@@ -143,6 +143,67 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
                            orb_build_info *info);
 
 /*
+ * Request server with continuous batching (no counterpart in the reference, which builds
+ * one tree per run). Instances stay resident on the GPU: their particles live in a device
+ * arena sized from hbm_budget_bytes; builds are admitted when their particles fit in the
+ * arena (otherwise they wait until orb_server_release frees memory), rebalances when their
+ * instance is idle. Each of `lanes` worker threads (own stream) takes every admissible
+ * pending request, up to max_batch (0 = no limit), into one batched build, so requests that
+ * arrive while others run are picked up by the next free lane and batches overlap on the
+ * device. Each instance's requests are applied in submission order; results are
+ * bit-identical to running the same requests one at a time.
+ */
+typedef struct orb_server orb_server;
+
+typedef struct orb_server_opts {
+    uint64_t hbm_budget_bytes; /* device memory for the arena and the lanes' scratch */
+    uint32_t max_batch;        /* most requests per batched build (0 = no limit) */
+    uint32_t lanes;            /* concurrent batches (0 = 2) */
+} orb_server_opts;
+
+typedef struct orb_request_result {
+    uint64_t request_id;
+    uint64_t instance_id; /* the id of the build request that created the instance */
+    int32_t status;       /* orb_status of the request */
+    int32_t kind;         /* 0 build, 1 rebalance */
+    uint32_t batch_size;  /* requests in the batched build that served it */
+    uint32_t pad_;
+    double submit_s, start_s, done_s; /* steady-clock seconds */
+} orb_request_result;
+
+typedef struct orb_server_stats {
+    uint64_t requests_submitted, requests_done, builds, rebalances, batches;
+    uint64_t particles_built, arena_particles, arena_used;
+    uint32_t max_batch_seen, pending;
+} orb_server_stats;
+
+orb_status orb_server_create(int device, const orb_server_opts *opts, orb_server **out);
+/* Stops the lanes (pending requests are dropped) and frees the device memory. */
+orb_status orb_server_destroy(orb_server *sv);
+/* New instance from host particles (copied at submission); instance id = *request_id. */
+orb_status orb_server_submit_build(orb_server *sv, const float *x, const float *y, const float *z,
+                                   uint64_t n, uint32_t d, uint32_t levels, const float lower[3],
+                                   const float upper[3], uint64_t *request_id);
+/* New instance from the seeded generator (orb_generate kinds), box [-0.5,0.5)^3. */
+orb_status orb_server_submit_generate(orb_server *sv, int kind, uint64_t seed, uint64_t n,
+                                      uint32_t d, uint32_t levels, uint64_t *request_id);
+/* Rebalance a resident instance: every coordinate += sigma * N(0,1) (seeded), clamped to the
+   instance's box, then the tree is rebuilt with the reference's rule. */
+orb_status orb_server_submit_rebalance(orb_server *sv, uint64_t instance_id, uint64_t seed,
+                                       float sigma, uint64_t *request_id);
+/* Blocks until the request finishes; returns its status. */
+orb_status orb_server_wait(orb_server *sv, uint64_t request_id, orb_request_result *out);
+/* Finished requests not yet polled (up to max). */
+orb_status orb_server_poll(orb_server *sv, orb_request_result *out, uint32_t max, uint32_t *n_out);
+/* Latest tree and particles of an instance (host buffers, each may be NULL): heap 2d-1 cells,
+   ranges 2(2d-1), x,y,z and the original index of the particle at each position (n). */
+orb_status orb_server_fetch(orb_server *sv, uint64_t instance_id, orb_cell_t *heap, uint32_t *ranges,
+                            float *x, float *y, float *z, uint32_t *ident);
+/* Frees the instance's arena slot after its pending requests finish. */
+orb_status orb_server_release(orb_server *sv, uint64_t instance_id);
+orb_status orb_server_get_stats(orb_server *sv, orb_server_stats *out);
+
+/*
  * Service layer: the reference's per-rank services over particles resident in the context.
  * orb_load_particles copies n particles in (host or device per flags), sets the range map
  * to root = [0, n) and sizes it for cell ids below max_cells.
