@@ -122,6 +122,23 @@ class ClockSampler:
                 "samples": len(sel)}
 
 
+def traffic_ratio(kernel: str):
+    """DRAM traffic per algorithmic byte of a kernel, from the committed ncu summary (a
+    smaller case of the same workload; the ratio is per swapped pair / per key, so it scales
+    with the units a launch processes)."""
+    names = {"part_swap": "k_part_swap", "count_left_hist": "k_hist", "part_classify": "k_part_classify"}
+    path = os.path.join(ROOT, "profiles", "dram_traffic_part_swap_hist_classify_2p24_2p12.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 3 and parts[0] == "traffic_per_algorithmic_byte" and parts[1] == names.get(kernel):
+                    return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
 def gpu_id_for(local_rank: int):
     cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
     if cvd:
@@ -441,10 +458,14 @@ def gpu_arm(args):
     achieved = dk["bytes"] / (dk["total_ms"] / 1e3) / 1e9
     kern_ms_total = sum(v["total_ms"] for v in warm_timed.values())
     dom_share = warm_timed[dom]["total_ms"] / kern_ms_total
+    ratio = traffic_ratio(dom)
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-        "traffic": None,
+        "traffic": (ratio * dk["bytes"] / dk["launches"]) if ratio else None,
+        "traffic_source": "ncu dram bytes per algorithmic byte, 2^24/2^12 capture scaled per unit"
+                          if ratio else None,
+        "dram_gbs_equivalent": round(achieved * ratio, 1) if ratio else None,
         "bytes_per_launch": dk["bytes"] / dk["launches"],
         "ms_per_launch": dk["total_ms"] / dk["launches"],
         "share_of_kernel_time": round(dom_share, 4),
