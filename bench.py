@@ -417,12 +417,9 @@ def gpu_arm(args):
     barrier()
     ms_total = ev0.elapsed_time(ev1)
     prof = ctx.profile()
-    if world > 1:
-        t = torch.tensor([ms_total])
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    import replicas
+    ms_total, _, value = replicas.whole_job(ms_total, n * args.steps)
     ms_step = ms_total / args.steps
-    value = n * world * args.steps / (ms_total / 1e3)
 
     # end to end through the C ABI with pinned host buffers
     hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
@@ -439,12 +436,8 @@ def gpu_arm(args):
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t)
     te1 = time.perf_counter()
-    e2e_s = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_s])
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = n * world * len(e2e_times) / e2e_s
+    e2e_ms, _, e2e_value = replicas.whole_job(1e3 * sum(e2e_times), n * len(e2e_times))
+    e2e_s = e2e_ms / 1e3
     clocks.stop()
 
     if rank != 0:
