@@ -380,13 +380,15 @@ def gpu_arm(args):
     heap_np = heap_pin.numpy().view(E.CELL_DTYPE)
     ranges_np = ranges_pin.numpy().view(np.uint32).reshape(-1, 2)
 
-    def step():
+    def step(with_perm=False):
+        # the reference's outputs: reordered x,y,z, cell heap, range map (it has no
+        # permutation output; with_perm adds the engine's optional one)
         x.copy_(x0)
         y.copy_(y0)
         z.copy_(z0)
         torch.cuda.synchronize(dev)
-        return ctx.build(x, y, z, d, perm=perm, device_pointers=True, heap_out=heap_np,
-                         ranges_out=ranges_np)
+        return ctx.build(x, y, z, d, perm=perm if with_perm else None, device_pointers=True,
+                         heap_out=heap_np, ranges_out=ranges_np)
 
     # warm-up steps time every kernel: per-kernel breakdown and the dominant kernel
     ctx.profile_reset(timing=True)
@@ -420,6 +422,17 @@ def gpu_arm(args):
     import replicas
     ms_total, _, value = replicas.whole_job(ms_total, n * args.steps)
     ms_step = ms_total / args.steps
+
+    # the same step with the optional permutation output (one more array moved per swap)
+    ctx.profile_reset(timing=False)
+    step(with_perm=True)
+    torch.cuda.synchronize(dev)
+    ev0.record()
+    for _ in range(args.steps):
+        step(with_perm=True)
+    ev1.record()
+    torch.cuda.synchronize(dev)
+    perm_ms_step = ev0.elapsed_time(ev1) / args.steps
 
     # end to end through the C ABI with pinned host buffers
     hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
@@ -493,8 +506,11 @@ def gpu_arm(args):
         "config": {"workload": WORKLOAD, "particles": n, "leaves": d, "levels": 16,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs 1.5 GB > 129 MB L2 (no flush needed)",
-                   "step": "d2d restore of x,y,z + orb_build (device pointers)"},
+                   "step": "d2d restore of x,y,z + orb_build (device pointers)",
+                   "outputs": "reordered x,y,z + cell heap + range map (as the reference; "
+                              "optional permutation off, timed separately as with_perm)"},
         "build_ms_device": statistics.median(i["device_ms"] for i in infos),
+        "with_perm_ms_per_step": round(perm_ms_step, 4),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 12 * n + heap_bytes + 8 * (2 * d - 1),
                 "call": "orb_build(x,y,z host pinned, perm=NULL): reordered x,y,z + heap + ranges back",

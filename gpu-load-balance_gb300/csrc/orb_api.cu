@@ -601,6 +601,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     }
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
+    if (!perm) v.idx = nullptr;  // no permutation asked for: only x, y, z move
     std::vector<LevelDesc> lv;
     for (uint32_t l = 1; l <= levels; ++l)
         lv.push_back({(1 << (l - 1)) - 1, nullptr, 1 << (l - 1)});  // src/orbit.cpp:104-107
@@ -1009,6 +1010,7 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
         ORB_CUDA(cudaMemcpyAsync(ctx->batch_slots.p, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
+    if (!perm) v.idx = nullptr;  // no permutation asked for: only x, y, z move
     for (uint32_t l = 1; l <= max_levels; ++l) {
         const size_t a = lv_off[l - 1], b = l < max_levels ? lv_off[l] : slots.size();
         lv.push_back({0, ctx->batch_slots.p + a, (int)(b - a)});

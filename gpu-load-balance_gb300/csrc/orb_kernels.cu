@@ -363,6 +363,33 @@ __device__ __forceinline__ int edge_bin(float k, float L, float scale, int top, 
     return lo;
 }
 
+// Margin of the scaled guess, in bins. The tree's edges deviate from the linear edges
+// L + j (R-L)/2^K by at most K u/2 <= 5.5u (every midpoint rounds once, to within u/2 of the
+// mean of its two endpoints; u = spacing of floats at max(|L|, |R|)). The guess
+// t = fl(fl(k-L) * scale), scale = fl(2^K / fl(R-L)), is within 1.01 u S + 2^K 2^-22 of the
+// exact (k-L) S, S = 2^K/(R-L). A fractional part of t farther than
+// m = 8 u scale + 2^K 2^-21 from 0 and 1 therefore puts k strictly between the edges of
+// bin floor(t). Returns 1 (guess never trusted) for non-finite or tiny brackets.
+__device__ __forceinline__ float bin_margin(float L, float R, float scale, uint32_t nb) {
+    const float M = fmaxf(fabsf(L), fabsf(R));
+    const int e = (__float_as_int(M) >> 23) & 0xff;
+    if (e < 24 || e == 0xff) return 1.0f;
+    const float u = __int_as_float((e - 23) << 23);
+    return __fadd_ru(__fmul_ru(__fmul_ru(8.0f, u), scale), __fmul_ru((float)nb, 0x1p-21f));
+}
+
+// edge_bin() with the scaled guess accepted outright when it is clear of both edges by the
+// margin m (bin_margin); L <= k < R.
+template <class EdgeAt>
+__device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, float one_m,
+                                        int top, EdgeAt e) {
+    const float t = __fmul_rn(__fsub_rn(k, L), scale);
+    const int g = __float2int_rz(t);
+    const float f = __fsub_rn(t, __int2float_rn(g));
+    if (g <= top && f > m && f < one_m) return g;
+    return edge_bin(k, L, scale, top, e);
+}
+
 // Keys per thread per round of the histogram pass (float4 loads issued together).
 constexpr int kHistVec = 4;
 
@@ -383,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
         const int K = v.hist_k[tr.c];
         const uint32_t nb = 1u << K;
         const int top = (int)nb - 1;
-        const float scale = __fdividef((float)nb, R - L);
+        const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
         const float *ge = cell_edges(v, tr.c);
         uint32_t *gh = v.hist + v.hist_off[tr.c];
         // Sparse pass: few keys of the cell lie in the bracket (known from the previous
@@ -397,6 +424,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
             }
             __syncthreads();
         }
+        const float m = bin_margin(L, R, scale, nb);
+        const float one_m = __fsub_rd(1.0f, m);
         uint32_t below = 0;
         auto visit = [&](float k) {
             if (k < L) {
@@ -406,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
                     const int g = edge_bin(k, L, scale, top, [&](int j) { return __ldg(ge + j); });
                     atomicAdd(&gh[g], 1u);
                 } else {
-                    const int g = edge_bin(k, L, scale, top, [&](int j) { return s_edge[j]; });
+                    const int g = fast_bin(k, L, scale, m, one_m, top, [&](int j) { return s_edge[j]; });
                     atomicAdd(&s_hist[g], 1u);
                 }
             }
@@ -817,11 +846,19 @@ __device__ __forceinline__ unsigned long long pack_status(unsigned long long fla
 }
 
 // P1: bitmasks of keys >= cut and keys <= cut per partition tile, and their counts.
+// One warp per tile: the metadata chains (tile -> cell -> range, cut) of the CTA's warps
+// overlap, and each lane keeps kClassifyLoads loads in flight. The mask words are staged in
+// shared memory and stored coalesced.
+constexpr int kClassifyLoads = 16;
+
 __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
-    __shared__ uint32_t s_cnt[2][kThreads / 32];
+    __shared__ uint32_t s_words[kThreads / 32][2][kPWords];
     const uint32_t total = v.ptile_off[v.C];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    uint32_t(*sw)[kPWords] = s_words[threadIdx.x >> 5];
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long bytes = 0;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < total; t += nwarps) {
         const int c = v.ptile_cell ? (int)v.ptile_cell[t] : find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c];
         const int slot = level_slot(v, c);
@@ -831,46 +868,45 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
         const uint2 rg = v.ranges[slot];
         const uint32_t p0 = rg.x + (t - t0) * (uint32_t)kPTile;
         const uint32_t m = min((uint32_t)kPTile, rg.y - p0);
+        uint32_t cg = 0, cl = 0;
+#pragma unroll 1
+        for (int r = 0; r < kPWords; r += kClassifyLoads) {
+            float k[kClassifyLoads];
+#pragma unroll
+            for (int u = 0; u < kClassifyLoads; ++u) {
+                const uint32_t i = (uint32_t)(r + u) * 32u + lane;
+                k[u] = i < m ? __ldg(keys + p0 + i) : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < kClassifyLoads; ++u) {
+                const int w = r + u;
+                const bool valid = (uint32_t)w * 32u + lane < m;
+                const uint32_t gb = __ballot_sync(0xffffffffu, valid && !(k[u] < cut));
+                const uint32_t lb = __ballot_sync(0xffffffffu, valid && !(k[u] > cut));
+                if (lane == u) {
+                    sw[0][w] = gb;
+                    sw[1][w] = lb;
+                }
+                cg += __popc(gb);
+                cl += __popc(lb);
+            }
+        }
         uint32_t *gw = v.ge_bits + (size_t)t * kPWords;
         uint32_t *lw = v.le_bits + (size_t)t * kPWords;
-        uint32_t cg = 0, cl = 0;
-        constexpr int kWordsPerWarp = kPWords / (kThreads / 32);
-        float k[kWordsPerWarp];
+        __syncwarp();
 #pragma unroll
-        for (int j = 0; j < kWordsPerWarp; ++j) {
-            const uint32_t i = (uint32_t)(warp * kWordsPerWarp + j) * 32u + lane;
-            k[j] = i < m ? __ldg(keys + p0 + i) : 0.0f;
+        for (int q = 0; q < kPWords / 32; ++q) {
+            gw[q * 32 + lane] = sw[0][q * 32 + lane];
+            lw[q * 32 + lane] = sw[1][q * 32 + lane];
         }
-#pragma unroll
-        for (int j = 0; j < kWordsPerWarp; ++j) {
-            const int w = warp * kWordsPerWarp + j;
-            const bool valid = (uint32_t)w * 32u + lane < m;
-            const uint32_t gb = __ballot_sync(0xffffffffu, valid && !(k[j] < cut));
-            const uint32_t lb = __ballot_sync(0xffffffffu, valid && !(k[j] > cut));
-            if (lane == 0) {
-                gw[w] = gb;
-                lw[w] = lb;
-            }
-            cg += __popc(gb);
-            cl += __popc(lb);
-        }
+        __syncwarp();
         if (lane == 0) {
-            s_cnt[0][warp] = cg;
-            s_cnt[1][warp] = cl;
+            v.pt_ge[t] = cg;
+            v.pt_le[t] = cl;
+            bytes += 4ull * m + 8ull * kPWords + 8ull;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t a = 0, b = 0;
-            for (int w = 0; w < kThreads / 32; ++w) {
-                a += s_cnt[0][w];
-                b += s_cnt[1][w];
-            }
-            v.pt_ge[t] = a;
-            v.pt_le[t] = b;
-            add_bytes(v, kKPartClassify, 4ull * m + 8ull * kPWords + 8ull);
-        }
-        __syncthreads();
     }
+    if (lane == 0 && bytes) add_bytes(v, kKPartClassify, bytes);
 }
 
 // P2: global exclusive prefix of the per-tile counts over every tile of the level:
@@ -1093,15 +1129,41 @@ __device__ __forceinline__ void swap_particles(const Level &v, uint32_t a, uint3
     }
 }
 
+// Largest u in [lo, hi] with pre[u] - base <= r, for a nondecreasing pre with
+// pre[lo] - base <= r: a 32-way search (every lane probes one point per round, the passing
+// probes are a prefix of the lanes), three rounds for 2^15 candidates. Warp-uniform result.
+__device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint32_t base,
+                                                      uint32_t lo, uint32_t hi, uint32_t r) {
+    const uint32_t lane = threadIdx.x & 31;
+    while (lo < hi) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t u = lo + (lane + 1) * step;
+        const bool ok = u <= hi && pre[u] - base <= r;
+        const uint32_t cnt = (uint32_t)__popc(__ballot_sync(0xffffffffu, ok));
+        lo += cnt * step;
+        hi = min(hi, lo + step - 1);
+    }
+    return lo;
+}
+
 // P4: the Hoare swaps. The CTA of tile t takes the pairs (L_k, R_k) whose left element
 // L_k lies in t (k < s); their right partners are the keys <= cut of left-to-right rank
 // le_tot-1-k, found in the right tiles' masks. Positions of each side are disjoint
 // (L_k < i <= R_k), so the CTAs never touch the same particle.
-__global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
+// Tuning (compile time): pairs per thread per round, and the CTAs per SM the register
+// budget is sized for (4 x 256 threads: 64 registers a thread).
+#ifndef ORB_SWAP_BATCH
+#define ORB_SWAP_BATCH 4
+#endif
+#ifndef ORB_SWAP_MIN_BLOCKS
+#define ORB_SWAP_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     __shared__ uint32_t posL[kPTile];
     __shared__ uint32_t posR[kPTile];
     __shared__ uint32_t sh[96];
     const uint32_t total = v.ptile_off[v.C];
+    unsigned long long bytes = 0;  // pairs swapped by this CTA
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const int c = v.ptile_cell ? (int)v.ptile_cell[t] : find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
@@ -1119,20 +1181,13 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
         // right partners: left-to-right <= ranks [le_tot-kb, le_tot-ka); rank r pairs with
         // k = le_tot-1-r, stored at posR[k - ka] = posR[(le_tot-1-ka) - r]
         const uint32_t ra = le_tot - kb, rb = le_tot - ka;
-        uint32_t u0 = t0, uh = t1 - 1;  // largest u with in-cell prefix <= ra
-        while (u0 < uh) {
-            const uint32_t mid = (u0 + uh + 1) >> 1;
-            if (v.pt_le_pre[mid] - L0 <= ra)
-                u0 = mid;
-            else
-                uh = mid - 1;
-        }
+        const uint32_t u0 = warp_last_at_most(v.pt_le_pre, L0, t0, t1 - 1, ra);
         for (uint32_t u = u0; u < t1 && v.pt_le_pre[u] - L0 < rb; ++u)
             emit_positions(v.le_bits + (size_t)u * kPWords, v.pt_le_pre[u] - L0, ra, rb,
                            (u - t0) * (uint32_t)kPTile, true, le_tot - 1 - ka, posR, sh);
         __syncthreads();
-        // four pairs per thread per round: every load is issued before any store
-        constexpr int kB = 4;
+        // kB pairs per thread per round: every load is issued before any store
+        constexpr int kB = ORB_SWAP_BATCH;
         for (uint32_t j0 = 0; j0 < cnt; j0 += kB * blockDim.x) {
             uint32_t pa[kB], pb[kB];
             float xa[kB], xb[kB], ya[kB], yb[kB], za[kB], zb[kB];
@@ -1171,9 +1226,11 @@ __global__ void __launch_bounds__(kThreads) k_part_swap(Level v) {
                 }
             }
         }
-        if (threadIdx.x == 0) add_bytes(v, kKPartSwap, 64ull * cnt);
+        bytes += cnt;
         __syncthreads();
     }
+    // per pair: both elements of x, y, z (and idx) read and written
+    if (threadIdx.x == 0 && bytes) add_bytes(v, kKPartSwap, (v.idx ? 64ull : 48ull) * bytes);
 }
 
 __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {

@@ -178,11 +178,13 @@ class Opts(ctypes.Structure):
 _lib = None
 
 
-def load(path: str = LIB_PATH):
-    """Load the engine library (it must already be built; see build())."""
+def load(path: str | None = None):
+    """Load the engine library (it must already be built; see build()). ORB_LIB may name
+    another build of it (kernel-parameter experiments)."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("ORB_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise OrbError(2, f"engine library not built: {path} (run __graft_entry__.build())")
     L = ctypes.CDLL(path)
