@@ -74,7 +74,6 @@ struct orb_ctx {
     int cta_min_cells = 0;  // levels with at least this many cells bisect one cell per CTA
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
-    DevBuf<float> edges;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
     DevBuf<unsigned long long> pt_status;
     DevBuf<int> slots;
@@ -177,7 +176,6 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->iters.ensure(max_cells));
     ORB_CUDA(ctx->slots.ensure(max_cells));
     ORB_CUDA(ctx->hist.ensure(max_bins, true));
-    ORB_CUDA(ctx->edges.ensure(max_bins + max_cells + 16));
     ORB_CUDA(ctx->ptile_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->counters.ensure(1, true));
     return ensure_ptile_buffers(ctx, max_ptiles);
@@ -201,7 +199,6 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.state = ctx->state.p;
     v.iters = ctx->iters.p;
     v.hist = ctx->hist.p;
-    v.edges = ctx->edges.p;
     v.below = ctx->below.p;
     v.inb = ctx->inb.p;
     v.ptile_off = ctx->ptile_off.p;
@@ -367,7 +364,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.heap, (const void *)v.ranges, (const void *)v.tile_off,
                           (const void *)v.hist_off, (const void *)v.hist_k, (const void *)v.state,
                           (const void *)v.iters, (const void *)v.hist, (const void *)v.below,
-                          (const void *)v.inb, (const void *)v.edges, (const void *)v.htile_cell,
+                          (const void *)v.inb, (const void *)v.htile_cell,
                           (const void *)v.ptile_cell, (const void *)v.ptile_off, (const void *)v.ge_bits,
                           (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
                           (const void *)v.pt_ge_pre, (const void *)v.pt_le_pre, (const void *)v.pt_status,
@@ -398,7 +395,7 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
 orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes) {
     for (int pass = 0; pass < kHistPasses; ++pass) {
         v.pass = pass;
-        run_kernel(ctx, kKHist, v, pass_grid(ctx));
+        run_kernel(ctx, kKHist, v, ctx->num_sms * kHistBlocksPerSm);
         run_kernel(ctx, kKResolve, v, pass_grid(ctx));
         ++*passes;
     }
@@ -429,7 +426,7 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
         } else {
             run_kernel(ctx, kKBisectWarp, v, 1);  // cells small enough for one warp
-            run_kernel(ctx, kKEdges, v, 1);
+            run_kernel(ctx, kKBisectTile, v, std::min(v.C, ctx->num_sms * 8));  // one-tile cells
             orb_status st = run_bisection(ctx, v, passes);
             if (st != ORB_OK) return st;
         }
@@ -537,7 +534,6 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release(); ctx->inb.release();
     ctx->part_s.release(); ctx->part_i.release(); ctx->part_le.release(); ctx->out_counts.release();
     ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
-    ctx->edges.release();
     ctx->ptile_off.release(); ctx->ge_bits.release(); ctx->le_bits.release(); ctx->pt_ge.release();
     ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release(); ctx->pt_status.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();

@@ -20,8 +20,10 @@ constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass
 // (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
 constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
+constexpr int kHistBlocksPerSm = 6;  // resident CTAs of the count-left pass (its grid)
 
-enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3 };
+// kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
+enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
 constexpr int kWarpKeys = 1024;      // cells up to this size bisect in one warp's registers
 
 // Kernel kinds, for launch counting, event timing and algorithmic-byte accounting.
@@ -37,10 +39,10 @@ enum Kernel : int {
     kKPartFinish,
     kKCountLeft,
     kKGenerate,
-    kKEdges,
     kKBisectCta,
     kKTileMap,
     kKBisectWarp,
+    kKBisectTile,
     kNumKernels
 };
 extern const char *const kKernelNames[kNumKernels];
@@ -77,7 +79,6 @@ struct Level {
     uint8_t *state;         // [C]   CellState
     uint8_t *iters;         // [C]   bisection iterations done
     uint32_t *hist;         // histogram pool (kept all-zero between passes)
-    float *edges;           // midpoint-tree edge tables, 2^K + 1 per cell at hist_off[c] + c
     uint32_t *below;        // [C]   keys below the left margin in the current pass
     uint32_t *inb;          // [C]   keys inside the current bracket (n before the first pass)
     // partition

@@ -23,8 +23,8 @@ namespace orb {
 
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
-    "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_edges",
-    "bisect_cta", "tile_map", "bisect_warp"};
+    "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
+    "tile_map", "bisect_warp", "bisect_tile"};
 
 namespace {
 
@@ -54,6 +54,18 @@ __device__ __forceinline__ uint32_t warp_min(uint32_t v) {
 }
 
 // Sum over the block; every thread gets the total. `sh` holds >= 32 words.
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) {
+    const int lane = threadIdx.x & 31;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    *total = __shfl_sync(0xffffffffu, inc, 31);
+    return inc - v;
+}
+
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_sum(v);
@@ -284,7 +296,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
         v.ptile_off[c] = pp;
         pp += (n + kPTile - 1) / kPTile;
         v.hist_k[c] = (uint8_t)k;
-        v.state[c] = n <= (uint32_t)kWarpKeys ? kSmall : kActive;
+        v.state[c] = n <= (uint32_t)kWarpKeys ? kSmall : (n <= (uint32_t)kTile ? kOneTile : kActive);
         v.iters[c] = 0;
         v.below[c] = 0;
         v.inb[c] = n;
@@ -301,38 +313,68 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
 // ------------------------------------------------------------------------------------
 // Count-left histogram pass
 // ------------------------------------------------------------------------------------
-// In-order edge table of the midpoint tree over [L, R] with 2^K leaves: e[0] = L,
-// e[2^K] = R, and e[j] = mid(e[j - s], e[j + s]) for the node j of stride s, i.e. exactly
-// the cut the reference's bisection computes at that node (src/cell.h:74-76). Built depth
-// by depth by one warp; __syncwarp orders the global writes between depths.
-__device__ void warp_edges(float *e, float L, float R, int K) {
+// The midpoint tree over [L, R] with nb = 2^K leaves: edge e(0) = L, e(nb) = R, and the
+// inner node j is the midpoint of its two nearest ancestors, i.e. exactly the cut the
+// reference's bisection computes at that node (src/cell.h:74-76).
+// Inner edges of the subtree of S leaves over [lo, hi] = [e(base), e(base + S)], written to
+// e[base .. base + S): each the midpoint of its two nearest ancestors, as in the full tree.
+template <int S>
+__device__ __forceinline__ void fill_sub(float *e, uint32_t base, float lo, float hi) {
+    float loc[S + 1];
+    loc[0] = lo;
+    loc[S] = hi;
+#pragma unroll
+    for (int st = S / 2; st >= 1; st /= 2) {
+#pragma unroll
+        for (int j = st; j < S; j += 2 * st) loc[j] = mid_cut(loc[j - st], loc[j + st]);
+    }
+#pragma unroll
+    for (int j = 0; j < S; ++j) e[base + j] = loc[j];
+}
+
+// Edge table e[0 .. 2^K] of the midpoint tree over [L, R], filled by nt threads (ti = this
+// thread's index, 2^K <= 16 nt): each descends once to the subtree of 2^K / nt leaves it
+// owns, then fills that subtree. The caller synchronises.
+__device__ void fill_edges(float *e, float L, float R, int K, uint32_t ti, uint32_t nt) {
     const uint32_t nb = 1u << K;
-    const uint32_t lane = threadIdx.x & 31;
-    if (lane == 0) {
-        e[0] = L;
-        e[nb] = R;
-    }
-    __syncwarp();
-    for (int d = 0; d < K; ++d) {
-        const uint32_t stride = nb >> (d + 1);
-        for (uint32_t i = lane; i < (1u << d); i += 32) {
-            const uint32_t j = (2 * i + 1) * stride;
-            e[j] = mid_cut(e[j - stride], e[j + stride]);
+    int ks = 0;
+    while ((nt << ks) < nb) ++ks;
+    const uint32_t S = 1u << ks, base = ti * S;
+    if (base < nb) {
+        float lo = L, hi = R;
+        for (int d = K - 1; d >= ks; --d) {
+            const float mm = mid_cut(lo, hi);
+            if (base & (1u << d))
+                lo = mm;
+            else
+                hi = mm;
         }
-        __syncwarp();
+        switch (ks) {
+            case 0: e[base] = lo; break;
+            case 1: fill_sub<2>(e, base, lo, hi); break;
+            case 2: fill_sub<4>(e, base, lo, hi); break;
+            case 3: fill_sub<8>(e, base, lo, hi); break;
+            default: fill_sub<16>(e, base, lo, hi); break;
+        }
     }
+    if (ti == 0) e[nb] = R;
 }
 
-__device__ __forceinline__ float *cell_edges(const Level &v, int c) {
-    return v.edges + v.hist_off[c] + c;
-}
-
-// Edge tables of every cell for the first histogram pass of a level (warp per cell).
-__global__ void __launch_bounds__(kThreads) k_edges(Level v) {
-    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (c >= v.C || v.state[c] != kActive) return;
-    const orb_cell_t &cell = v.heap[level_slot(v, c)];
-    warp_edges(cell_edges(v, c), cell.cutMarginLeft, cell.cutMarginRight, v.hist_k[c]);
+// Leaf of key k (L <= k < R) in that tree: the reference's descent itself (k below the
+// midpoint: left half, else right half), K midpoints.
+__device__ __forceinline__ int tree_bin(float k, float L, float R, int K) {
+    float lo = L, hi = R;
+    int b = 0;
+    for (int d = K - 1; d >= 0; --d) {
+        const float mm = mid_cut(lo, hi);
+        if (k < mm) {
+            hi = mm;
+        } else {
+            lo = mm;
+            b += 1 << d;
+        }
+    }
+    return b;
 }
 
 // Bin of key k (L <= k < R) in the edge table e[0..nb]: the largest b with e[b] <= k, i.e.
@@ -378,95 +420,129 @@ __device__ __forceinline__ float bin_margin(float L, float R, float scale, uint3
     return __fadd_ru(__fmul_ru(__fmul_ru(8.0f, u), scale), __fmul_ru((float)nb, 0x1p-21f));
 }
 
+// edge_bin() over a table in shared memory, out of line: it runs for a few keys only, and
+// the streaming loops that call it stay small enough for the instruction cache.
+__device__ __noinline__ int edge_bin_slow(float k, float L, float scale, int top, const float *e) {
+    return edge_bin(k, L, scale, top, [&](int j) { return e[j]; });
+}
+
 // edge_bin() with the scaled guess accepted outright when it is clear of both edges by the
 // margin m (bin_margin); L <= k < R.
-template <class EdgeAt>
 __device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, float one_m,
-                                        int top, EdgeAt e) {
+                                        int top, const float *e) {
     const float t = __fmul_rn(__fsub_rn(k, L), scale);
     const int g = __float2int_rz(t);
     const float f = __fsub_rn(t, __int2float_rn(g));
     if (g <= top && f > m && f < one_m) return g;
-    return edge_bin(k, L, scale, top, e);
+    return edge_bin_slow(k, L, scale, top, e);
+}
+
+// One bracket key of a sparse pass into the cell's global bins (out of line, as above).
+__device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R, int K) {
+    atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
 }
 
 // Keys per thread per round of the histogram pass (float4 loads issued together).
 constexpr int kHistVec = 4;
 
-__global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
+constexpr int kGroup = 4 * kHistVec;  // keys a thread holds per round
+
+// Group visitor that applies a per-key visitor to each key in order.
+template <class Visit>
+__device__ __forceinline__ auto each(Visit &visit) {
+    return [&visit](const float (&k)[kGroup]) {
+#pragma unroll
+        for (int i = 0; i < kGroup; ++i) visit(k[i]);
+    };
+}
+
+// Keys [e0, e1) of one axis, visited by `nt` threads (ti = this thread's index): scalar
+// head to 16-byte alignment and scalar tail through visit(k), float4 body (kHistVec loads
+// in flight a thread) through group(k[kGroup]). `pad` fills the body's missing lanes and
+// must be a value the visitors ignore.
+template <class Visit, class Group>
+__device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint32_t e1, float pad,
+                                           uint32_t ti, uint32_t nt, Visit visit, Group group) {
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
+    const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
+    for (uint32_t i = e0 + ti; i < a0; i += nt) visit(__ldg(keys + i));
+    const uint32_t n4 = (e1 - a0) >> 2;
+    const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
+    for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * nt) {
+        float4 q[kHistVec];
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            const uint32_t j = j0 + u * nt + ti;
+            q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
+        }
+        float k[kGroup];
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            k[4 * u] = q[u].x;
+            k[4 * u + 1] = q[u].y;
+            k[4 * u + 2] = q[u].z;
+            k[4 * u + 3] = q[u].w;
+        }
+        group(k);
+    }
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(__ldg(keys + i));
+}
+
+// One count-left pass over the tiles of the level's active cells (cells of more than one
+// tile; a tile loop over all CTAs). Dense cells are binned into a shared-memory histogram
+// added to the cell's global bins; sparse cells (few keys in the bracket, known from the
+// previous pass) send their bracket keys straight to the global bins.
+__global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
     __shared__ uint32_t s_hist[1 << kMaxBinsLog2];
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
-    __shared__ uint32_t s_red[32];
+    __shared__ uint32_t s_red[96];
     if (blockIdx.x == 0 && threadIdx.x == 0) v.counters->any_active[v.pass & 1] = 0u;
     // every cell of the level finished in an earlier pass: nothing to bin
     if (v.pass > 0 && *(volatile uint32_t *)&v.counters->any_active[(v.pass - 1) & 1] == 0u) return;
     const uint32_t total = v.tile_off[v.C];
+    unsigned long long bytes = 0;
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const TileRef tr = tile_ref(v, t);
         if (v.state[tr.c] != kActive) continue;
         const orb_cell_t &cell = v.heap[tr.slot];
-        const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+        const uint32_t cell_tiles = v.tile_off[tr.c + 1] - v.tile_off[tr.c];
+        const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
         const int K = v.hist_k[tr.c];
         const uint32_t nb = 1u << K;
         const int top = (int)nb - 1;
         const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
-        const float *ge = cell_edges(v, tr.c);
         uint32_t *gh = v.hist + v.hist_off[tr.c];
-        // Sparse pass: few keys of the cell lie in the bracket (known from the previous
-        // pass), so they go straight to the global bins; dense pass: shared-memory bins.
-        const uint32_t cell_tiles = v.tile_off[tr.c + 1] - v.tile_off[tr.c];
         const bool sparse = v.inb[tr.c] <= 64u * cell_tiles;
         if (!sparse) {
-            for (uint32_t j = threadIdx.x; j <= nb; j += blockDim.x) {
-                if (j < nb) s_hist[j] = 0u;
-                s_edge[j] = ge[j];
-            }
+            for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) s_hist[j] = 0u;
+            fill_edges(s_edge, L, R, K, threadIdx.x, blockDim.x);
             __syncthreads();
         }
         const float m = bin_margin(L, R, scale, nb);
         const float one_m = __fsub_rd(1.0f, m);
         uint32_t below = 0;
-        auto visit = [&](float k) {
-            if (k < L) {
-                ++below;
-            } else if (k < R) {
-                if (sparse) {
-                    const int g = edge_bin(k, L, scale, top, [&](int j) { return __ldg(ge + j); });
-                    atomicAdd(&gh[g], 1u);
-                } else {
-                    const int g = fast_bin(k, L, scale, m, one_m, top, [&](int j) { return s_edge[j]; });
-                    atomicAdd(&s_hist[g], 1u);
-                }
-            }
-        };
-        // keys [e0, e1): scalar head to 16-byte alignment, float4 body, scalar tail
-        const uint32_t e0 = tr.e0, e1 = tr.e1;
-        const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
-        const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
-        for (uint32_t i = e0 + threadIdx.x; i < a0; i += blockDim.x) visit(__ldg(keys + i));
-        const uint32_t n4 = (e1 - a0) >> 2;
-        const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
-        for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * blockDim.x) {
-            float4 q[kHistVec];
-#pragma unroll
-            for (int u = 0; u < kHistVec; ++u) {
-                const uint32_t j = j0 + u * blockDim.x + threadIdx.x;
-                q[u] = j < n4 ? __ldg(k4 + j) : make_float4(R, R, R, R);  // R: never counted
-            }
-#pragma unroll
-            for (int u = 0; u < kHistVec; ++u) {
-                visit(q[u].x);
-                visit(q[u].y);
-                visit(q[u].z);
-                visit(q[u].w);
-            }
+        if (sparse) {
+            auto one = [&](float k) {
+                if (k < L)
+                    ++below;
+                else if (k < R)
+                    add_sparse(gh, k, L, R, K);
+            };
+            visit_keys(keys, tr.e0, tr.e1, R, threadIdx.x, blockDim.x, one, each(one));
+        } else {
+            auto one = [&](float k) {
+                if (k < L)
+                    ++below;
+                else if (k < R)
+                    atomicAdd(&s_hist[fast_bin(k, L, scale, m, one_m, top, s_edge)], 1u);
+            };
+            visit_keys(keys, tr.e0, tr.e1, R, threadIdx.x, blockDim.x, one, each(one));
         }
-        for (uint32_t i = a0 + (n4 << 2) + threadIdx.x; i < e1; i += blockDim.x) visit(__ldg(keys + i));
         below = block_sum(below, s_red);
         if (threadIdx.x == 0) {
             if (below) atomicAdd(&v.below[tr.c], below);
-            add_bytes(v, kKHist, 4ull * (e1 - e0));
+            bytes += 4ull * (tr.e1 - tr.e0);
         }
         if (!sparse) {
             for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -476,6 +552,158 @@ __global__ void __launch_bounds__(kThreads, 8) k_hist(Level v) {
             __syncthreads();
         }
     }
+    if (threadIdx.x == 0 && bytes) add_bytes(v, kKHist, bytes);
+}
+
+// ------------------------------------------------------------------------------------
+// Bisection of one-tile cells (kWarpKeys < n <= kTile keys): one warp per cell, the whole
+// reference loop (src/orbit.cpp:146-232) in one launch. Histogram rounds over the midpoint
+// tree of the current bracket (about 16 keys a bin, warp-private shared-memory bins) each
+// replay up to K iterations on the prefix counts; once the bracket holds at most
+// kListKeys keys they are gathered into registers and every remaining iteration is a
+// register count plus a warp sum. Every round streams the cell's keys (L2-resident after
+// the first).
+// ------------------------------------------------------------------------------------
+constexpr int kTileBinsLog2 = 9;
+constexpr int kTileBins = 1 << kTileBinsLog2;
+constexpr int kListPerLane = 8;     // bracket keys a lane can hold
+constexpr uint32_t kListKeys = 64;  // bracket size that switches to the register list
+
+__global__ void __launch_bounds__(kThreads, 4) k_bisect_tile(Level v) {
+    __shared__ uint32_t s_bins[kThreads / 32][kTileBins];
+    __shared__ float s_edges[kThreads / 32][kTileBins + 1];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *bins = s_bins[warp];
+    float *edges = s_edges[warp];
+    const int nwarps = (int)(gridDim.x * (blockDim.x >> 5));
+    unsigned long long bytes = 0;
+    for (int c = (int)(blockIdx.x * (blockDim.x >> 5) + warp); c < v.C; c += nwarps) {
+        if (v.state[c] != kOneTile) continue;
+        const int slot = level_slot(v, c);
+        orb_cell_t &cell = v.heap[slot];
+        const uint2 rg = v.ranges[slot];
+        const uint32_t n = rg.y - rg.x;
+        const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+        float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+        uint32_t it = 0, cand = n;
+        int st = kActive;
+        while (st == kActive) {
+            bytes += 4ull * n;
+            if (cand <= kListKeys) {
+                // the bracket's keys into registers (each lane keeps its own), keys below L
+                float kl[kListPerLane];
+                uint32_t nk = 0, below = 0;
+                bool over = false;
+                auto gather = [&](float k) {
+                    if (k < L) {
+                        ++below;
+                    } else if (k < R) {
+                        if (nk < (uint32_t)kListPerLane) {
+#pragma unroll
+                            for (int q = 0; q < kListPerLane; ++q)
+                                if (q == (int)nk) kl[q] = k;
+                        } else {
+                            over = true;
+                        }
+                        ++nk;
+                    }
+                };
+                visit_keys(keys, rg.x, rg.y, R, lane, 32, gather, each(gather));
+                if (!__any_sync(0xffffffffu, over)) {
+                    below = warp_sum(below);
+                    while (st == kActive) {
+                        if (it >= (uint32_t)kMaxIterations) {
+                            st = kCapped;
+                            break;
+                        }
+                        const float cut = mid_cut(L, R);
+                        uint32_t cnt = 0;
+#pragma unroll
+                        for (int q = 0; q < kListPerLane; ++q) cnt += (q < (int)nk) && kl[q] < cut;
+                        const uint32_t cl = below + warp_sum(cnt);
+                        ++it;
+                        const int dir = convergence(cl, n);
+                        if (dir == 0)
+                            st = kFound;
+                        else if (dir > 0)
+                            R = cut;
+                        else
+                            L = cut;
+                    }
+                    break;
+                }
+                // a lane met more than it can hold: one more histogram round instead
+            }
+            const int K = max(1, min(kTileBinsLog2, 28 - __clz(max(cand, 1u))));
+            const uint32_t nb = 1u << K;
+            for (uint32_t j = lane; j < nb; j += 32) bins[j] = 0u;
+            fill_edges(edges, L, R, K, lane, 32);
+            __syncwarp();
+            const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
+            const float m = bin_margin(L, R, scale, nb);
+            const float one_m = __fsub_rd(1.0f, m);
+            const int top = (int)nb - 1;
+            uint32_t below = 0;
+            auto one = [&](float k) {
+                if (k < L)
+                    ++below;
+                else if (k < R)
+                    atomicAdd(&bins[fast_bin(k, L, scale, m, one_m, top, edges)], 1u);
+            };
+            visit_keys(keys, rg.x, rg.y, R, lane, 32, one, each(one));
+            __syncwarp();
+            below = warp_sum(below);
+            // exclusive prefix of the bins in place (each lane its own run of bins)
+            const uint32_t per = max(1u, nb >> 5), j0 = lane * per, j1 = min(nb, j0 + per);
+            uint32_t loc = 0;
+            for (uint32_t j = j0; j < j1; ++j) loc += bins[j];
+            uint32_t tot;
+            uint32_t run = warp_excl_scan(loc, &tot);
+            for (uint32_t j = j0; j < j1; ++j) {
+                const uint32_t h = bins[j];
+                bins[j] = run;
+                run += h;
+            }
+            __syncwarp();
+            // replay up to K iterations (identically in every lane)
+            uint32_t pos = 0, width = nb;
+            for (int step = 0; step < K; ++step) {
+                if (it >= (uint32_t)kMaxIterations) {
+                    st = kCapped;
+                    break;
+                }
+                const uint32_t half = width >> 1;
+                const uint32_t cl = below + bins[pos + half];
+                ++it;
+                const int dir = convergence(cl, n);
+                if (dir == 0) {
+                    st = kFound;
+                    break;
+                }
+                const float cut = mid_cut(L, R);
+                if (dir > 0) {
+                    R = cut;
+                } else {
+                    L = cut;
+                    pos += half;
+                }
+                width = half;
+            }
+            if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
+            if (st == kActive) cand = (pos + 1 < nb ? bins[pos + 1] : tot) - bins[pos];
+            __syncwarp();  // the bins are rewritten by the next round
+        }
+        if (lane == 0) {
+            cell.cutMarginLeft = L;
+            cell.cutMarginRight = R;
+            cell.foundCut = st == kFound ? 1 : 0;
+            v.iters[c] = (uint8_t)it;
+            v.state[c] = (uint8_t)st;
+            atomicMax(&v.counters->max_iters, it);
+            if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+        }
+    }
+    if (lane == 0 && bytes) add_bytes(v, kKBisectTile, bytes);
 }
 
 // ------------------------------------------------------------------------------------
@@ -527,10 +755,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     const uint32_t next_inb = g[pos];  // keys in the bracket the next pass would bin
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
-    if (st == kActive) {
-        if (lane == 0) v.inb[c] = next_inb;
-        warp_edges(cell_edges(v, c), L, R, K);  // tree of the next pass
-    }
+    if (st == kActive && lane == 0) v.inb[c] = next_inb;
     if (lane == 0) {
         add_bytes(v, kKResolve, 8ull << K);  // bins read and cleared
         cell.cutMarginLeft = L;
@@ -652,34 +877,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
             const int K = max(1, min(kMaxBinsLog2, 32 - __clz(max(cand, 1u))));
             const uint32_t nb = 1u << K;
             for (uint32_t j = tid; j < kBins; j += blockDim.x) s_hist[j] = 0u;
-            for (uint32_t j = tid; j <= nb; j += blockDim.x) {
-                float e;
-                if (j == 0) {
-                    e = L;
-                } else if (j == nb) {
-                    e = R;
-                } else {
-                    float lo = L, hi = R;
-                    uint32_t b0 = 0, span = nb;
-                    for (;;) {
-                        const uint32_t half = span >> 1;
-                        const float mm = mid_cut(lo, hi);
-                        const uint32_t idx = b0 + half;
-                        if (j == idx) {
-                            e = mm;
-                            break;
-                        }
-                        if (j < idx) {
-                            hi = mm;
-                        } else {
-                            lo = mm;
-                            b0 = idx;
-                        }
-                        span = half;
-                    }
-                }
-                s_edge[j] = e;
-            }
+            fill_edges(s_edge, L, R, K, tid, blockDim.x);
             __syncthreads();
             const float scale = __fdividef((float)nb, R - L);
             uint32_t below = 0;
@@ -740,7 +938,8 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
             }
             if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
             if (st != kActive) break;
-            inb = s_hist[pos + 1] - s_hist[pos];  // keys in the new bracket [L, R)
+            // keys in the new bracket [L, R) (entry nb of the prefix is the round's total)
+            inb = (pos + 1 < nb ? s_hist[pos + 1] : tot_a) - s_hist[pos];
             __syncthreads();
             // ---- the new bracket's keys become the candidates
             if (in_list) {
@@ -821,17 +1020,6 @@ __device__ __forceinline__ float cell_cut(const orb_cell_t &c) {
     return mid_cut(c.cutMarginLeft, c.cutMarginRight);
 }
 
-__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) {
-    const int lane = threadIdx.x & 31;
-    uint32_t inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    *total = __shfl_sync(0xffffffffu, inc, 31);
-    return inc - v;
-}
 
 // Status word of one scan block in the look-back: flag (bits 62-63), count of keys
 // >= cut (bits 31-61) and keys <= cut (bits 0-30). Level totals stay below 2^31.
@@ -1468,15 +1656,13 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
     switch (k) {
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
         case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKBisectCta:
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;
         case kKTileMap: k_tile_map<<<grid, kThreads, 0, st>>>(v); break;
         case kKBisectWarp:
             k_bisect_warp<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-            break;
-        case kKEdges:
-            k_edges<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
         case kKResolve:
             k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
