@@ -437,6 +437,8 @@ __device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, 
     return edge_bin_slow(k, L, scale, top, e);
 }
 
+
+
 // One bracket key of a sparse pass into the cell's global bins (out of line, as above).
 __device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R, int K) {
     atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
@@ -446,6 +448,49 @@ __device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R,
 constexpr int kHistVec = 4;
 
 constexpr int kGroup = 4 * kHistVec;  // keys a thread holds per round
+
+// The keys [e0, e1) of one tile (at most kTile keys), visited by the CTA's threads. The
+// float4 body goes through settle(k, i) (i = the key's slot in its round), branch-free code
+// that handles the common case and returns false for a key it leaves; those are remembered
+// by one bit each and visited afterwards through rest(k), and the unaligned head and tail
+// through visit(k). `pad` fills the body's missing lanes: settle(pad) must count nothing
+// (a pad it leaves is skipped by the walk).
+static_assert(kTile / (4 * kHistVec * kThreads) <= 4, "scan_tile keeps 16 bits a round, 4 rounds");
+template <class Settle, class Rest, class Visit>
+__device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32_t e1, float pad,
+                                          Settle settle, Rest rest, Visit visit) {
+    const uint32_t ti = threadIdx.x, nt = blockDim.x;
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
+    const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
+    for (uint32_t i = e0 + ti; i < a0; i += nt) visit(__ldg(keys + i));
+    const uint32_t n4 = (e1 - a0) >> 2;
+    const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
+    unsigned long long left = 0;  // bit 16 r + 4 u + c: component c of load u of round r
+    uint32_t r = 0;
+    for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * nt, ++r) {
+        float4 q[kHistVec];
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            const uint32_t j = j0 + u * nt + ti;
+            q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
+        }
+        uint32_t miss = 0;
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            const float kk[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) miss |= (uint32_t)!settle(kk[c]) << (4 * u + c);
+        }
+        left |= (unsigned long long)miss << (16u * r);
+    }
+    while (left) {
+        const int b = __ffsll((long long)left) - 1;
+        left &= left - 1;
+        const uint32_t j = (uint32_t)(b >> 4) * (kHistVec * nt) + (uint32_t)((b >> 2) & 3) * nt + ti;
+        if (j < n4) rest(__ldg(keys + a0 + 4 * j + (b & 3)));  // else a pad lane
+    }
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(__ldg(keys + i));
+}
 
 // Group visitor that applies a per-key visitor to each key in order.
 template <class Visit>
@@ -493,9 +538,9 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
 // added to the cell's global bins; sparse cells (few keys in the bracket, known from the
 // previous pass) send their bracket keys straight to the global bins.
 __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
-    __shared__ uint32_t s_hist[1 << kMaxBinsLog2];
+    __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
-    __shared__ uint32_t s_red[96];
+    __shared__ uint32_t s_red[32];
     if (blockIdx.x == 0 && threadIdx.x == 0) v.counters->any_active[v.pass & 1] = 0u;
     // every cell of the level finished in an earlier pass: nothing to bin
     if (v.pass > 0 && *(volatile uint32_t *)&v.counters->any_active[(v.pass - 1) & 1] == 0u) return;
@@ -523,21 +568,44 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         const float one_m = __fsub_rd(1.0f, m);
         uint32_t below = 0;
         if (sparse) {
-            auto one = [&](float k) {
-                if (k < L)
-                    ++below;
-                else if (k < R)
-                    add_sparse(gh, k, L, R, K);
-            };
-            visit_keys(keys, tr.e0, tr.e1, R, threadIdx.x, blockDim.x, one, each(one));
+            // sparse: keys below L counted, keys in [L, R) (few) binned afterwards
+            scan_tile(
+                keys, tr.e0, tr.e1, R,
+                [&](float k) {
+                    below += k < L;
+                    return !(k >= L && k < R);
+                },
+                [&](float k) { add_sparse(gh, k, L, R, K); },
+                [&](float k) {
+                    if (k < L)
+                        ++below;
+                    else if (k < R)
+                        add_sparse(gh, k, L, R, K);
+                });
         } else {
-            auto one = [&](float k) {
+            // dense: the scaled guess alone, no range test (a key below L gives a guess below
+            // bin 0 or a fraction <= m, one at or above R a guess past the top bin or a
+            // fraction >= 1 - m, NaN fails every comparison); a key it does not settle is
+            // counted in the lane's spare bin past the top (never read) and binned exactly
+            // afterwards
+            const int spare = top + 1 + (int)(threadIdx.x & 31);
+            auto exact = [&](float k) {
                 if (k < L)
                     ++below;
                 else if (k < R)
-                    atomicAdd(&s_hist[fast_bin(k, L, scale, m, one_m, top, s_edge)], 1u);
+                    atomicAdd(&s_hist[edge_bin_slow(k, L, scale, top, s_edge)], 1u);
             };
-            visit_keys(keys, tr.e0, tr.e1, R, threadIdx.x, blockDim.x, one, each(one));
+            scan_tile(
+                keys, tr.e0, tr.e1, R,
+                [&](float k) {
+                    const float t = __fmul_rn(__fsub_rn(k, L), scale);
+                    const int g = __float2int_rz(t);
+                    const float f = __fsub_rn(t, __int2float_rn(g));
+                    const bool ok = g <= top && f > m && f < one_m;
+                    atomicAdd(&s_hist[ok ? g : spare], 1u);
+                    return ok;
+                },
+                exact, exact);
         }
         below = block_sum(below, s_red);
         if (threadIdx.x == 0) {
