@@ -20,7 +20,7 @@ constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass
 // (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
 constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
-constexpr int kHistBlocksPerSm = 6;  // resident CTAs of the count-left pass (its grid)
+constexpr int kHistBlocksPerSm = 8;  // resident CTAs of the count-left pass (its grid)
 
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
