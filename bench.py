@@ -263,6 +263,12 @@ def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
         return (time.perf_counter() - t) / steps, r
 
     ctx.profile_reset(timing=False)
+    # launch parameters chosen by the engine's autotuner on this batch (every candidate's
+    # trees checked equal); both forms below run under the chosen setting
+    default_tuning = ctx.get_tuning()
+    t0 = time.perf_counter()
+    tuning, tuned_ms = ctx.autotune_batch(x0, y0, z0, inst, reps=3, device_pointers=True)
+    tune_s = time.perf_counter() - t0
     t_batch, (parts, _, binfo) = timed(batch_step)
     bperm = perm.cpu().numpy()
     t_plain, _ = timed(plain_step)
@@ -279,6 +285,8 @@ def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
         "ms_per_batch": 1e3 * t_batch, "ms_plain_one_at_a_time": 1e3 * t_plain,
         "particles_per_s": total / t_batch,
         "bit_exact_vs_plain": bool(same),
+        "autotune": {"chosen": tuning, "default": default_tuning,
+                     "median_build_ms": round(tuned_ms, 3), "tuning_s": round(tune_s, 2)},
     }
 
 
@@ -389,6 +397,13 @@ def gpu_arm(args):
         torch.cuda.synchronize(dev)
         return ctx.build(x, y, z, d, perm=perm if with_perm else None, device_pointers=True,
                          heap_out=heap_np, ranges_out=ranges_np)
+
+    # launch parameters from the engine's autotuner on this workload (before any timing; the
+    # inputs are copied, every candidate's tree is checked equal)
+    t0 = time.perf_counter()
+    tuning, _ = ctx.autotune_batch(x0, y0, z0, [{"offset": 0, "n": n, "d": d}], reps=2,
+                                   device_pointers=True)
+    tune_s = time.perf_counter() - t0
 
     # warm-up steps time every kernel: per-kernel breakdown and the dominant kernel
     ctx.profile_reset(timing=True)
@@ -510,6 +525,7 @@ def gpu_arm(args):
                    "outputs": "reordered x,y,z + cell heap + range map (as the reference; "
                               "optional permutation off, timed separately as with_perm)"},
         "build_ms_device": statistics.median(i["device_ms"] for i in infos),
+        "tuning": {"chosen": tuning, "by": "orb_autotune_batch", "tuning_s": round(tune_s, 2)},
         "with_perm_ms_per_step": round(perm_ms_step, 4),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 12 * n + heap_bytes + 8 * (2 * d - 1),

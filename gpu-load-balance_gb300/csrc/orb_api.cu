@@ -71,7 +71,8 @@ struct orb_ctx {
     DevBuf<uint2> ranges;
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint32_t> htile_cell, ptile_cell;
-    int cta_min_cells = 0;  // levels with at least this many cells bisect one cell per CTA
+    // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
+    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u};
     DevBuf<uint8_t> hist_k, state, iters;
     DevBuf<uint32_t> hist;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
@@ -81,6 +82,7 @@ struct orb_ctx {
     DevBuf<orb_cell_t> staging;
     DevBuf<BatchRoot> batch_roots;
     DevBuf<int> batch_slots;
+    DevBuf<float> tune_src[3], tune_work[3];  // autotuner: input copy, build arrays
     BuildCounters *h_counters = nullptr;  // pinned
 
     // service layer state
@@ -214,11 +216,12 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.part_i = ctx->part_i.p;
     v.part_le = ctx->part_le.p;
     v.out_counts = ctx->out_counts.p;
+    v.sparse_per_tile = ctx->tune.sparse_keys_per_tile;
     v.counters = ctx->counters.p;
     return v;
 }
 
-int pass_grid(orb_ctx *ctx) { return ctx->num_sms * 8; }
+int pass_grid(orb_ctx *ctx) { return ctx->num_sms * (int)ctx->tune.part_blocks_per_sm; }
 
 cudaEvent_t take_event(orb_ctx *ctx) {
     if (!ctx->ev_pool.empty()) {
@@ -373,7 +376,9 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
         key_add(key, p);
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
-    key.push_back((uint64_t)ctx->cta_min_cells);
+    for (uint32_t t : {ctx->tune.hist_blocks_per_sm, ctx->tune.part_blocks_per_sm, ctx->tune.tile_blocks_per_sm,
+                       ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells})
+        key.push_back(t);
     return key;
 }
 
@@ -395,7 +400,7 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
 orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes) {
     for (int pass = 0; pass < kHistPasses; ++pass) {
         v.pass = pass;
-        run_kernel(ctx, kKHist, v, ctx->num_sms * kHistBlocksPerSm);
+        run_kernel(ctx, kKHist, v, ctx->num_sms * (int)ctx->tune.hist_blocks_per_sm);
         run_kernel(ctx, kKResolve, v, pass_grid(ctx));
         ++*passes;
     }
@@ -421,12 +426,12 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         if (v.C == 0) continue;
         run_kernel(ctx, kKPlan, v, 1);
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
-        if (v.C >= ctx->cta_min_cells) {
+        if (ctx->tune.cta_min_cells && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
             // many cells: one CTA bisects one cell, no host round trip
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
         } else {
             run_kernel(ctx, kKBisectWarp, v, 1);  // cells small enough for one warp
-            run_kernel(ctx, kKBisectTile, v, std::min(v.C, ctx->num_sms * 8));  // one-tile cells
+            run_kernel(ctx, kKBisectTile, v, std::min(v.C, ctx->num_sms * (int)ctx->tune.tile_blocks_per_sm));
             orb_status st = run_bisection(ctx, v, passes);
             if (st != ORB_OK) return st;
         }
@@ -498,7 +503,7 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             const char *env = std::getenv("ORB_CTA_MIN_CELLS");
             // Measured on GB300 (2^27 particles, 2^16 leaves): the multi-CTA histogram passes
             // beat one-CTA-per-cell at every level, so the CTA path is opt-in.
-            ctx->cta_min_cells = env ? std::atoi(env) : 1 << 30;
+            ctx->tune.cta_min_cells = env ? (uint32_t)std::max(0, std::atoi(env)) : 0u;
             const char *ng = std::getenv("ORB_NO_GRAPHS");
             ctx->use_graphs = !(ng && ng[0] && ng[0] != '0');
         }
@@ -539,6 +544,10 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     ctx->htile_cell.release(); ctx->ptile_cell.release();
     ctx->batch_roots.release(); ctx->batch_slots.release();
+    for (int a = 0; a < 3; ++a) {
+        ctx->tune_src[a].release();
+        ctx->tune_work[a].release();
+    }
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
     drop_all_graphs(ctx);
@@ -1088,6 +1097,132 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
         info->h2d_ms = h2d_ms;
         info->d2h_ms = d2h_ms;
     }
+    return ORB_OK;
+}
+
+orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out) {
+    if (!ctx || !out) return ORB_ERR_INVALID_ARGUMENT;
+    *out = ctx->tune;
+    return ORB_OK;
+}
+
+static bool tuning_valid(const orb_tuning &t) {
+    return t.hist_blocks_per_sm >= 1 && t.hist_blocks_per_sm <= (uint32_t)kHistBlocksPerSm &&
+           t.part_blocks_per_sm >= 1 && t.part_blocks_per_sm <= 16 && t.tile_blocks_per_sm >= 1 &&
+           t.tile_blocks_per_sm <= (uint32_t)kTileBlocksPerSm && t.sparse_keys_per_tile >= 1 &&
+           t.sparse_keys_per_tile <= (uint32_t)kTile;
+}
+
+orb_status orb_set_tuning(orb_ctx *ctx, const orb_tuning *t) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!t || !tuning_valid(*t)) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "tuning parameter out of range");
+    ctx->tune = *t;
+    return ORB_OK;
+}
+
+orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, const float *z,
+                              uint64_t n_total, const orb_batch_instance *inst, uint32_t k,
+                              uint32_t flags, uint32_t reps, orb_tuning *best, float *best_ms) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
+    if (!best || !best_ms || reps < 1 || reps > 100 || k == 0 || !inst ||
+        (n_total > 0 && (!x || !y || !z)))
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer, no instances or reps outside 1..100");
+    if (n_total >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "n_total must be below 2^31");
+    const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
+    if (dev && n_total > 0 && (!is_device_ptr(x) || !is_device_ptr(y) || !is_device_ptr(z)))
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "ORB_DEVICE_POINTERS set but a pointer is not device memory");
+    uint64_t heap_cells = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (inst[i].d == 0 || inst[i].d > (1u << 30)) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance d");
+        heap_cells += 2ull * inst[i].d - 1;
+    }
+    ORB_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const float *in[3] = {x, y, z};
+    for (int a = 0; a < 3; ++a) {
+        ORB_CUDA(ctx->tune_src[a].ensure(n_total + 1));
+        ORB_CUDA(ctx->tune_work[a].ensure(n_total + 1));
+        if (n_total)
+            ORB_CUDA(cudaMemcpyAsync(ctx->tune_src[a].p, in[a], n_total * sizeof(float),
+                                     dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    }
+    std::vector<orb_cell_t> heaps(heap_cells), ref_heaps;
+    std::vector<uint32_t> ranges(2 * heap_cells), ref_ranges;
+    // median device time of `reps` builds (after one untimed build: graph capture)
+    auto trial = [&](const orb_tuning &t, float *ms) -> orb_status {
+        ctx->tune = t;
+        std::vector<float> times;
+        for (uint32_t r = 0; r <= reps; ++r) {
+            for (int a = 0; a < 3; ++a)
+                if (n_total)
+                    ORB_CUDA(cudaMemcpyAsync(ctx->tune_work[a].p, ctx->tune_src[a].p,
+                                             n_total * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            orb_build_info info;
+            orb_status st = orb_build_batch(ctx, ctx->tune_work[0].p, ctx->tune_work[1].p,
+                                            ctx->tune_work[2].p, n_total, inst, k, heaps.data(),
+                                            ranges.data(), nullptr, ORB_DEVICE_POINTERS, &info);
+            if (st != ORB_OK) return st;
+            if (r == 0) {
+                if (ref_heaps.empty()) {
+                    ref_heaps = heaps;
+                    ref_ranges = ranges;
+                } else if (std::memcmp(ref_heaps.data(), heaps.data(), heaps.size() * sizeof(orb_cell_t)) ||
+                           ref_ranges != ranges) {
+                    return fail(ctx, ORB_ERR_CUDA, "autotune: a candidate setting built a different tree");
+                }
+            } else {
+                times.push_back(info.device_ms);
+            }
+        }
+        std::sort(times.begin(), times.end());
+        *ms = times[times.size() / 2];
+        return ORB_OK;
+    };
+    const orb_tuning start = ctx->tune;
+    orb_tuning cur = start;
+    float cur_ms = 0.f;
+    orb_status st = trial(cur, &cur_ms);
+    if (st != ORB_OK) {
+        ctx->tune = start;
+        return st;
+    }
+    // coordinate descent over result-invariant parameters
+    static const uint32_t hist_c[] = {4, 6, 8}, part_c[] = {4, 8, 16}, tile_c[] = {2, 4},
+                          sparse_c[] = {16, 64, 256}, cta_c[] = {0, 512, 4096};
+    struct Axis {
+        uint32_t orb_tuning::*field;
+        const uint32_t *vals;
+        int n;
+    };
+    const Axis axes[] = {{&orb_tuning::hist_blocks_per_sm, hist_c, 3},
+                         {&orb_tuning::part_blocks_per_sm, part_c, 3},
+                         {&orb_tuning::tile_blocks_per_sm, tile_c, 2},
+                         {&orb_tuning::sparse_keys_per_tile, sparse_c, 3},
+                         {&orb_tuning::cta_min_cells, cta_c, 3}};
+    for (const Axis &ax : axes) {
+        const orb_tuning base = cur;
+        for (int i = 0; i < ax.n; ++i) {
+            if (ax.vals[i] == base.*ax.field) continue;
+            orb_tuning t = base;
+            t.*ax.field = ax.vals[i];
+            float ms = 0.f;
+            st = trial(t, &ms);
+            if (st != ORB_OK) {
+                ctx->tune = start;
+                return st;
+            }
+            if (ms < 0.98f * cur_ms) {  // keep a candidate only for a clear gain
+                cur = t;
+                cur_ms = ms;
+            }
+        }
+    }
+    ctx->tune = cur;
+    *best = cur;
+    *best_ms = cur_ms;
     return ORB_OK;
 }
 

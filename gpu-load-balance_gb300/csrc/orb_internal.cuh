@@ -20,7 +20,8 @@ constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass
 // (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
 constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
-constexpr int kHistBlocksPerSm = 8;  // resident CTAs of the count-left pass (its grid)
+constexpr int kHistBlocksPerSm = 8;  // resident CTAs of the count-left pass (most useful grid)
+constexpr int kTileBlocksPerSm = 4;  // resident CTAs of the one-tile cell bisection
 
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
@@ -95,6 +96,7 @@ struct Level {
     uint32_t *part_i;       // [C] split index (cell-relative); n when clamped
     uint32_t *part_le;      // [C] keys <= cut in the cell
     uint32_t *out_counts;   // service calls: per-cell result
+    uint32_t sparse_per_tile;  // count pass: sparse once the bracket holds <= this x tiles keys
     BuildCounters *counters;
 };
 

@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         const int top = (int)nb - 1;
         const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
         uint32_t *gh = v.hist + v.hist_off[tr.c];
-        const bool sparse = v.inb[tr.c] <= 64u * cell_tiles;
+        const bool sparse = v.inb[tr.c] <= v.sparse_per_tile * cell_tiles;
         if (!sparse) {
             for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) s_hist[j] = 0u;
             fill_edges(s_edge, L, R, K, threadIdx.x, blockDim.x);
@@ -637,7 +637,7 @@ constexpr int kTileBins = 1 << kTileBinsLog2;
 constexpr int kListPerLane = 8;     // bracket keys a lane can hold
 constexpr uint32_t kListKeys = 64;  // bracket size that switches to the register list
 
-__global__ void __launch_bounds__(kThreads, 4) k_bisect_tile(Level v) {
+__global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Level v) {
     __shared__ uint32_t s_bins[kThreads / 32][kTileBins];
     __shared__ float s_edges[kThreads / 32][kTileBins + 1];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

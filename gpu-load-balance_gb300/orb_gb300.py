@@ -65,7 +65,8 @@ EXPORTS = [
     "orb_profile_reset", "orb_profile_read", "orb_count_left_static", "orb_build_batch",
     "orb_profile_kernel_index", "orb_server_create", "orb_server_destroy", "orb_server_submit_build",
     "orb_server_submit_generate", "orb_server_submit_rebalance", "orb_server_wait", "orb_server_poll",
-    "orb_server_fetch", "orb_server_release", "orb_server_get_stats",
+    "orb_server_fetch", "orb_server_release", "orb_server_get_stats", "orb_get_tuning",
+    "orb_set_tuning", "orb_autotune_batch",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -118,6 +119,20 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+class Tuning(ctypes.Structure):
+    """orb_tuning: launch parameters that never change a result."""
+    _fields_ = [
+        ("hist_blocks_per_sm", ctypes.c_uint32),
+        ("part_blocks_per_sm", ctypes.c_uint32),
+        ("tile_blocks_per_sm", ctypes.c_uint32),
+        ("sparse_keys_per_tile", ctypes.c_uint32),
+        ("cta_min_cells", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
 
 
 class BuildInfo(ctypes.Structure):
@@ -225,6 +240,13 @@ def load(path: str | None = None):
     L.orb_profile_kernel_index.argtypes = [ctypes.c_char_p]
     L.orb_profile_read.restype = ctypes.c_int
     L.orb_profile_read.argtypes = [vp, ctypes.POINTER(KernelStat), ctypes.c_int]
+    L.orb_get_tuning.restype = ctypes.c_int
+    L.orb_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.orb_set_tuning.restype = ctypes.c_int
+    L.orb_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.orb_autotune_batch.restype = ctypes.c_int
+    L.orb_autotune_batch.argtypes = [vp, vp, vp, vp, u64, ctypes.POINTER(BatchInstance), u32, u32, u32,
+                                     ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_float)]
     L.orb_build_batch.restype = ctypes.c_int
     L.orb_build_batch.argtypes = [vp, vp, vp, vp, u64, ctypes.POINTER(BatchInstance), u32, vp, vp,
                                   vp, u32, ctypes.POINTER(BuildInfo)]
@@ -334,9 +356,8 @@ class Context:
         self._check(st)
         return BuildResult(heap, ranges, perm, info.as_dict())
 
-    def build_batch(self, x, y, z, instances, perm=True, device_pointers: bool = False):
-        """Batched build. `instances`: list of dicts {offset, n, d, levels=0, lower, upper}.
-        Returns (list of per-instance (heap, ranges) views, perm, info)."""
+    @staticmethod
+    def _instances(instances):
         k = len(instances)
         arr = (BatchInstance * max(k, 1))()
         heap_cells = 0
@@ -352,6 +373,40 @@ class Context:
                 b.upper[a] = ins.get("upper", (0.5, 0.5, 0.5))[a]
             bases.append(heap_cells)
             heap_cells += 2 * b.d - 1
+        return arr, heap_cells, bases
+
+    # launch tuning -----------------------------------------------------------------
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(self.lib.orb_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **params):
+        """Change some tuning parameters (the rest keep their current values)."""
+        t = Tuning()
+        self._check(self.lib.orb_get_tuning(self.h, ctypes.byref(t)))
+        for k, v in params.items():
+            setattr(t, k, int(v))
+        self._check(self.lib.orb_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune_batch(self, x, y, z, instances, reps: int = 3, device_pointers: bool = False):
+        """Autotune the launch parameters on a batch (inputs are not modified). Returns
+        (chosen tuning dict, its median build ms)."""
+        arr, _, _ = self._instances(instances)
+        n_total = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        best = Tuning()
+        ms = ctypes.c_float()
+        self._check(self.lib.orb_autotune_batch(self.h, _ptr(x), _ptr(y), _ptr(z), n_total, arr,
+                                                len(instances),
+                                                ORB_DEVICE_POINTERS if device_pointers else 0,
+                                                reps, ctypes.byref(best), ctypes.byref(ms)))
+        return best.as_dict(), float(ms.value)
+
+    def build_batch(self, x, y, z, instances, perm=True, device_pointers: bool = False):
+        """Batched build. `instances`: list of dicts {offset, n, d, levels=0, lower, upper}.
+        Returns (list of per-instance (heap, ranges) views, perm, info)."""
+        k = len(instances)
+        arr, heap_cells, bases = self._instances(instances)
         n_total = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
         heaps = np.zeros(max(heap_cells, 1), CELL_DTYPE)
         ranges = np.zeros((max(heap_cells, 1), 2), np.uint32)

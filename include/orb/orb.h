@@ -143,6 +143,39 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
                            orb_build_info *info);
 
 /*
+ * Launch tuning of a context (no counterpart in the reference). Every parameter changes
+ * only how the work is spread over the GPU, never a result: trees, ranges and particle
+ * order are the same under any valid setting.
+ */
+typedef struct orb_tuning {
+    uint32_t hist_blocks_per_sm;   /* count-left pass: CTAs per SM, 1..8 (default 8) */
+    uint32_t part_blocks_per_sm;   /* partition passes: CTAs per SM, 1..16 (default 8) */
+    uint32_t tile_blocks_per_sm;   /* one-tile cell bisection: CTAs per SM, 1..4 (default 4) */
+    uint32_t sparse_keys_per_tile; /* compaction threshold: a count pass sends a cell's bracket
+                                      keys straight to its global bins (instead of binning all
+                                      keys in shared memory) once the bracket holds at most
+                                      this many keys per tile, 1..16384 (default 64) */
+    uint32_t cta_min_cells;        /* levels with at least this many cells bisect one cell per
+                                      CTA; 0 = never (default) */
+} orb_tuning;
+
+orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out);
+orb_status orb_set_tuning(orb_ctx *ctx, const orb_tuning *t); /* ORB_ERR_INVALID_ARGUMENT
+                                                                 outside the ranges above */
+
+/*
+ * Autotuner: times batched builds of the given instances (x,y,z host or, with
+ * ORB_DEVICE_POINTERS, device arrays; they are copied, never modified) under candidate
+ * settings, one parameter at a time (coordinate descent from the current setting), `reps`
+ * builds per candidate (median device time), and checks that every candidate builds the
+ * same trees. The fastest setting becomes the context's; it is returned in *best with its
+ * median build time in *best_ms.
+ */
+orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, const float *z,
+                              uint64_t n_total, const orb_batch_instance *inst, uint32_t k,
+                              uint32_t flags, uint32_t reps, orb_tuning *best, float *best_ms);
+
+/*
  * Request server with continuous batching (no counterpart in the reference, which builds
  * one tree per run). Instances stay resident on the GPU: their particles live in a device
  * arena sized from hbm_budget_bytes; builds are admitted when their particles fit in the

@@ -49,6 +49,16 @@ def test_cell_layout(engine):
     assert dt.itemsize == 52
 
 
+def test_tuning_layout_and_null_checks(engine):
+    # orb_tuning: five uint32 fields, no padding
+    assert ctypes.sizeof(engine.Tuning) == 20
+    lib = engine.load()
+    t = engine.Tuning()
+    assert lib.orb_get_tuning(None, ctypes.byref(t)) == 1
+    assert lib.orb_set_tuning(None, ctypes.byref(t)) == 1
+    assert lib.orb_autotune_batch(None, None, None, None, 0, None, 0, 0, 1, None, None) == 1
+
+
 def test_invalid_arguments_without_device(engine):
     lib = engine.load()
     # null out-pointer is rejected before any CUDA call
