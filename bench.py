@@ -126,7 +126,8 @@ def traffic_ratio(kernel: str):
     """DRAM traffic per algorithmic byte of a kernel, from the committed ncu summary (a
     smaller case of the same workload; the ratio is per swapped pair / per key, so it scales
     with the units a launch processes)."""
-    names = {"part_swap": "k_part_swap", "count_left_hist": "k_hist", "part_classify": "k_part_classify"}
+    names = {"part_swap": "k_part_swap", "count_left_hist": "k_hist", "part_classify": "k_part_classify",
+             "bisect_tile": "k_bisect_tile"}
     path = os.path.join(ROOT, "profiles", "dram_traffic_part_swap_hist_classify_2p24_2p12.txt")
     try:
         with open(path) as f:
@@ -401,8 +402,15 @@ def gpu_arm(args):
     # launch parameters from the engine's autotuner on this workload (before any timing; the
     # inputs are copied, every candidate's tree is checked equal)
     t0 = time.perf_counter()
-    tuning, _ = ctx.autotune_batch(x0, y0, z0, [{"offset": 0, "n": n, "d": d}], reps=2,
-                                   device_pointers=True)
+    if args.tuning:
+        names = ("hist_blocks_per_sm", "part_blocks_per_sm", "tile_blocks_per_sm",
+                 "sparse_keys_per_tile", "cta_min_cells")
+        ctx.set_tuning(**dict(zip(names, (int(v) for v in args.tuning.split(",")))))
+        tuning, tuned_by = ctx.get_tuning(), "--tuning"
+    else:
+        tuning, _ = ctx.autotune_batch(x0, y0, z0, [{"offset": 0, "n": n, "d": d}], reps=2,
+                                       device_pointers=True)
+        tuned_by = "orb_autotune_batch"
     tune_s = time.perf_counter() - t0
 
     # warm-up steps time every kernel: per-kernel breakdown and the dominant kernel
@@ -525,7 +533,7 @@ def gpu_arm(args):
                    "outputs": "reordered x,y,z + cell heap + range map (as the reference; "
                               "optional permutation off, timed separately as with_perm)"},
         "build_ms_device": statistics.median(i["device_ms"] for i in infos),
-        "tuning": {"chosen": tuning, "by": "orb_autotune_batch", "tuning_s": round(tune_s, 2)},
+        "tuning": {"chosen": tuning, "by": tuned_by, "tuning_s": round(tune_s, 2)},
         "with_perm_ms_per_step": round(perm_ms_step, 4),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 12 * n + heap_bytes + 8 * (2 * d - 1),
@@ -558,6 +566,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help="hist,part,tile,sparse,cta: use this launch tuning for the headline "
+                         "instead of autotuning it (profiling runs reuse a chosen setting)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
