@@ -1,0 +1,93 @@
+"""CPU check of the count pass's scaled-guess binning (k_hist, k_bisect_tile): whenever the
+guess is accepted by the margin test it is the exact leaf of the midpoint tree, i.e. the bin
+the reference's bisection descent reaches. float32 restatement of the device arithmetic; the
+margin here uses round-to-nearest (the device rounds it up), so it accepts at least as many
+guesses as the device does."""
+import numpy as np
+
+f32 = np.float32
+
+
+def midpoint_edges(L, R, K):
+    """Edge table e[0..2^K] of the midpoint tree over [L, R] (float32 midpoints, in order)."""
+    nb = 1 << K
+    e = np.empty(nb + 1, f32)
+    e[0], e[nb] = L, R
+    for d in range(K):
+        s = nb >> (d + 1)
+        j = np.arange(s, nb, 2 * s)
+        e[j] = (e[j + s] + e[j - s]) * f32(0.5)  # mid_cut: fl(fl(R + L) * 0.5)
+    return e
+
+
+def margin(L, R, scale, nb):
+    M = max(abs(L), abs(R))
+    e = int(np.array(M, f32).view(np.uint32)) >> 23 & 0xFF
+    if e < 24 or e == 0xFF:
+        return f32(1.0)
+    u = np.array((e - 23) << 23, np.uint32).view(f32)[()]
+    return f32(f32(f32(8.0) * u) * scale) + f32(f32(nb) * f32(2.0 ** -21))
+
+
+def check_bracket(rng, L, R, K, nkeys):
+    nb = 1 << K
+    e = midpoint_edges(L, R, K)
+    scale = f32(nb) / f32(R - L)
+    m = margin(L, R, scale, nb)
+    one_m = f32(1.0) - m
+    # keys: uniform in [L, R), plus edges and their float neighbours
+    k = (f32(L) + f32(R - L) * rng.random(nkeys).astype(f32)).astype(f32)
+    j = rng.integers(0, nb + 1, nkeys // 4)
+    near = np.concatenate([e[j], np.nextafter(e[j], f32(np.inf)), np.nextafter(e[j], f32(-np.inf))])
+    k = np.concatenate([k, near.astype(f32)])
+    k = k[(k >= L) & (k < R)]
+    t = (k - f32(L)).astype(f32) * scale
+    g = np.trunc(t).astype(np.int64)
+    fr = (t - g.astype(f32)).astype(f32)
+    ok = (g <= nb - 1) & (fr > m) & (fr < one_m)
+    exact = np.searchsorted(e[:nb], k, side="right") - 1  # largest b with e[b] <= k
+    bad = ok & (g != exact)
+    return int(ok.sum()), int(bad.sum()), len(k)
+
+
+def test_accepted_guesses_are_exact():
+    rng = np.random.default_rng(5)
+    accepted = total = 0
+    for trial in range(400):
+        K = int(rng.integers(4, 12))
+        mode = trial % 4
+        if mode == 0:  # boxes of the unit cube and their sub-brackets
+            L = f32(-0.5 + (rng.integers(0, 1 << 24) * 2.0 ** -24))
+            R = f32(L + f32(2.0 ** -int(rng.integers(0, 20))))
+        elif mode == 1:  # anywhere, any width
+            L = f32(rng.uniform(-1e3, 1e3))
+            R = f32(L + f32(10.0 ** rng.uniform(-5, 2)))
+        elif mode == 2:  # a few hundred ulps wide
+            L = f32(rng.uniform(-1, 1))
+            R = L
+            for _ in range(int(rng.integers(1, 400))):
+                R = np.nextafter(R, f32(np.inf))
+        else:  # straddling zero
+            w = f32(10.0 ** rng.uniform(-6, 0))
+            L = f32(-w * f32(rng.random()))
+            R = f32(L + w)
+        if not (L < R) or not np.isfinite(R - L):
+            continue
+        a, bad, n = check_bracket(rng, L, R, K, 4000)
+        assert bad == 0, f"guess off its exact bin in [{L!r}, {R!r}) K={K}"
+        accepted += a
+        total += n
+    assert accepted > 0
+
+
+def test_guess_settles_almost_every_key_of_a_box():
+    # the first pass of the unit box: uniform keys, 2048 bins
+    rng = np.random.default_rng(6)
+    L, R, K = f32(-0.5), f32(0.5), 11
+    nb = 1 << K
+    scale = f32(nb) / f32(R - L)
+    m = margin(L, R, scale, nb)
+    k = (L + f32(R - L) * rng.random(200000).astype(f32)).astype(f32)
+    t = (k - L).astype(f32) * scale
+    fr = (t - np.trunc(t).astype(f32)).astype(f32)
+    assert ((fr > m) & (fr < f32(1.0) - m)).mean() > 0.99
