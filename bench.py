@@ -37,6 +37,7 @@ N_PARTICLES = 1 << 27
 LEAVES = 1 << 16
 SEED = 20270
 METRIC = "orb_build_particles_per_s"
+WARM_WIDTH = 8.0  # warm rebuild: bracket factor (half-width = factor x extent / sqrt(n))
 UNIT = "particles/s"
 WORKLOAD = "plain ORB, 2^27 uniform float32 particles in [-0.5,0.5)^3, 2^16 leaf cells"
 FALLBACK_HBM_GBS = 6800.0
@@ -457,6 +458,36 @@ def gpu_arm(args):
     torch.cuda.synchronize(dev)
     perm_ms_step = ev0.elapsed_time(ev1) / args.steps
 
+    # warm-started rebuild (labelled mode, not bit-identical with a cold build): the same
+    # particles displaced by sigma = 1e-3 (seeded, clamped to the box), rebuilt cold and from
+    # the previous tree's cuts
+    warm_rb = None
+    if rank == 0:
+        prev_heap = heap_np.copy()  # the tree of x0,y0,z0 (last step above)
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED + 11)
+        hi = float(np.nextafter(np.float32(0.5), np.float32(0)))
+        xd, yd, zd = ((a + 1e-3 * torch.randn(n, generator=g, device=dev)).clamp_(-0.5, hi)
+                      for a in (x0, y0, z0))
+        cold_ms, warm_ms, winfo = [], [], None
+        for i in range(args.warmup + args.steps):
+            for dst, src in ((x, xd), (y, yd), (z, zd)):
+                dst.copy_(src)
+            c = ctx.build(x, y, z, d, perm=None, device_pointers=True)
+            for dst, src in ((x, xd), (y, yd), (z, zd)):
+                dst.copy_(src)
+            w = ctx.build_warm(x, y, z, d, prev_heap, WARM_WIDTH, perm=None, device_pointers=True)
+            if i >= args.warmup:
+                cold_ms.append(c.info["device_ms"])
+                warm_ms.append(w.info["device_ms"])
+                winfo = w.info
+        warm_rb = {"workload": f"{WORKLOAD}, particles displaced by N(0, 1e-3^2) per coordinate",
+                "width": WARM_WIDTH, "cold_build_ms": round(statistics.median(cold_ms), 3),
+                "warm_build_ms": round(statistics.median(warm_ms), 3),
+                "speedup": round(statistics.median(cold_ms) / statistics.median(warm_ms), 3),
+                "warm_cells": winfo["warm_cells"], "warm_resets": winfo["warm_resets"],
+                "note": "labelled mode: a valid ORB tree, not bit-identical with the cold build"}
+
     # end to end through the C ABI with pinned host buffers
     hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
     hx.copy_(x0.cpu()); hy.copy_(y0.cpu()); hz.copy_(z0.cpu())
@@ -535,6 +566,7 @@ def gpu_arm(args):
         "build_ms_device": statistics.median(i["device_ms"] for i in infos),
         "tuning": {"chosen": tuning, "by": tuned_by, "tuning_s": round(tune_s, 2)},
         "with_perm_ms_per_step": round(perm_ms_step, 4),
+        "warm_rebuild": warm_rb,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 12 * n + heap_bytes + 8 * (2 * d - 1),
                 "call": "orb_build(x,y,z host pinned, perm=NULL): reordered x,y,z + heap + ranges back",

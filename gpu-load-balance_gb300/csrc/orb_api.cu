@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <list>
 #include <mutex>
 #include <new>
@@ -83,6 +84,9 @@ struct orb_ctx {
     DevBuf<BatchRoot> batch_roots;
     DevBuf<int> batch_slots;
     DevBuf<float> tune_src[3], tune_work[3];  // autotuner: input copy, build arrays
+    DevBuf<float2> hint;      // warm builds: starting bracket per heap slot
+    DevBuf<int> hint_axis;
+    DevBuf<uint8_t> warm;
     BuildCounters *h_counters = nullptr;  // pinned
 
     // service layer state
@@ -425,8 +429,9 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         v.C = d.C;
         if (v.C == 0) continue;
         run_kernel(ctx, kKPlan, v, 1);
+        if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
-        if (ctx->tune.cta_min_cells && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
+        if (ctx->tune.cta_min_cells && !v.hint && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
             // many cells: one CTA bisects one cell, no host round trip
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
         } else {
@@ -548,6 +553,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
         ctx->tune_src[a].release();
         ctx->tune_work[a].release();
     }
+    ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
     drop_all_graphs(ctx);
@@ -665,6 +671,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         info->device_ms = dev_ms;
         info->h2d_ms = h2d_ms;
         info->d2h_ms = d2h_ms;
+        info->warm_cells = ctx->h_counters->warm_cells;
+        info->warm_resets = ctx->h_counters->warm_resets;
     }
     return ORB_OK;
 }
@@ -926,10 +934,13 @@ orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells
 // ---------------------------------------------------------------------------------------
 // Batched builds
 // ---------------------------------------------------------------------------------------
-orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
-                           const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
-                           uint32_t *ranges, uint32_t *perm, uint32_t flags,
-                           orb_build_info *info) {
+// Batched build; with prev_heaps, a warm build (widths[i] > 0: instance i's cells start from
+// the previous tree's cuts, see orb_build_batch_warm).
+static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                                   const orb_batch_instance *inst, uint32_t k,
+                                   const orb_cell_t *prev_heaps, const float *widths,
+                                   orb_cell_t *heaps, uint32_t *ranges, uint32_t *perm,
+                                   uint32_t flags, orb_build_info *info) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
     if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
@@ -1010,18 +1021,56 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
         }
         ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
     }
+    bool warm = false;
+    if (prev_heaps) {
+        // starting brackets from the previous trees on the cut axis: cut +- w x extent / sqrt(n)
+        std::vector<float2> hint(heap_cells);
+        std::vector<int> hint_axis(heap_cells, -2);
+        const float nan = std::numeric_limits<float>::quiet_NaN();
+        for (uint32_t i = 0; i < k; ++i) {
+            const uint64_t hb = roots[i].heap_base, hc = 2ull * inst[i].d - 1;
+            for (uint64_t j = 0; j < hc; ++j) {
+                hint[hb + j] = make_float2(nan, nan);
+                const orb_cell_t &p = prev_heaps[hb + j];
+                if (!(widths[i] > 0.f) || p.nLeafCells < 2 || p.cutAxis < 0 || p.cutAxis > 2) continue;
+                const int a = p.cutAxis;
+                const float cut = (p.cutMarginRight + p.cutMarginLeft) * 0.5f;
+                // (cut, w x extent); the device divides the extent part by sqrt(n) of the cell
+                const float wext = widths[i] * (p.upper[a] - p.lower[a]);
+                if (!std::isfinite(cut) || !std::isfinite(wext)) continue;
+                hint[hb + j] = make_float2(cut, wext);
+                hint_axis[hb + j] = a;
+                warm = true;
+            }
+        }
+        if (warm) {
+            ORB_CUDA(ctx->hint.ensure(heap_cells + 1));
+            ORB_CUDA(ctx->hint_axis.ensure(heap_cells + 1));
+            ORB_CUDA(ctx->warm.ensure(max_cells + 1));
+            ORB_CUDA(cudaMemcpyAsync(ctx->hint.p, hint.data(), heap_cells * sizeof(float2), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaMemcpyAsync(ctx->hint_axis.p, hint_axis.data(), heap_cells * sizeof(int), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+        }
+    }
     if (k) ORB_CUDA(cudaMemcpyAsync(ctx->batch_roots.p, roots.data(), k * sizeof(BatchRoot), cudaMemcpyHostToDevice, s));
     if (!slots.empty())
         ORB_CUDA(cudaMemcpyAsync(ctx->batch_slots.p, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
     if (!perm) v.idx = nullptr;  // no permutation asked for: only x, y, z move
+    if (warm) {
+        v.hint = ctx->hint.p;
+        v.hint_axis = ctx->hint_axis.p;
+        v.warm = ctx->warm.p;
+    }
     for (uint32_t l = 1; l <= max_levels; ++l) {
         const size_t a = lv_off[l - 1], b = l < max_levels ? lv_off[l] : slots.size();
         lv.push_back({0, ctx->batch_slots.p + a, (int)(b - a)});
     }
     std::vector<uint64_t> key = level_key(ctx, v);
-    key.push_back(0xBA7C4);  // batched build
+    key.push_back(warm ? 0xBA7C4A : 0xBA7C4);  // batched build (warm)
+    key_add(key, v.hint);
+    key_add(key, v.warm);
     key.push_back(n_total);
     key_add(key, ctx->batch_roots.p);
     key_add(key, ctx->batch_slots.p);
@@ -1096,8 +1145,54 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
         info->device_ms = dev_ms;
         info->h2d_ms = h2d_ms;
         info->d2h_ms = d2h_ms;
+        info->warm_cells = ctx->h_counters->warm_cells;
+        info->warm_resets = ctx->h_counters->warm_resets;
     }
     return ORB_OK;
+}
+
+orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                           const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
+                           uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                           orb_build_info *info) {
+    return build_batch_impl(ctx, x, y, z, n_total, inst, k, nullptr, nullptr, heaps, ranges, perm,
+                            flags, info);
+}
+
+orb_status orb_build_batch_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                                const orb_batch_instance *inst, uint32_t k,
+                                const orb_cell_t *prev_heaps, const float *widths,
+                                orb_cell_t *heaps, uint32_t *ranges, uint32_t *perm,
+                                uint32_t flags, orb_build_info *info) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (k > 0 && (!prev_heaps || !widths)) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null prev_heaps or widths");
+    for (uint32_t i = 0; i < k; ++i)
+        if (!(widths[i] >= 0.f) || !std::isfinite(widths[i]))
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "widths must be finite and >= 0");
+    return build_batch_impl(ctx, x, y, z, n_total, inst, k, prev_heaps, widths, heaps, ranges, perm,
+                            flags, info);
+}
+
+orb_status orb_build_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                          uint32_t levels, const float lower[3], const float upper[3],
+                          const orb_cell_t *prev_heap, float width, orb_cell_t *heap_out,
+                          uint32_t *ranges_out, uint32_t *perm, uint32_t flags,
+                          orb_build_info *info) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (!lower || !upper) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null box");
+    orb_batch_instance b;
+    b.offset = 0;
+    b.n = n;
+    b.d = d;
+    b.levels = levels;
+    for (int a = 0; a < 3; ++a) {
+        b.lower[a] = lower[a];
+        b.upper[a] = upper[a];
+    }
+    return orb_build_batch_warm(ctx, x, y, z, n, &b, 1, prev_heap, &width, heap_out, ranges_out, perm,
+                                flags, info);
 }
 
 orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out) {

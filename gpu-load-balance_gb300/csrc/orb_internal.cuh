@@ -44,6 +44,7 @@ enum Kernel : int {
     kKTileMap,
     kKBisectWarp,
     kKBisectTile,
+    kKWarmStart,
     kNumKernels
 };
 extern const char *const kKernelNames[kNumKernels];
@@ -57,6 +58,8 @@ struct BuildCounters {
     uint32_t any_active[2];  // pass p: cleared by hist p, set by resolve p if a cell goes on
     uint32_t error;       // set when a bounded device wait gave up
     uint32_t ticket;      // block ticket of the tile scan (reset before each launch)
+    uint32_t warm_cells;  // warm builds: cells that started from a hinted bracket
+    uint32_t warm_resets; // ... whose hinted bracket missed the target (restarted cold)
     unsigned long long bytes[16];  // algorithmic bytes per Kernel kind
 };
 
@@ -97,6 +100,11 @@ struct Level {
     uint32_t *part_le;      // [C] keys <= cut in the cell
     uint32_t *out_counts;   // service calls: per-cell result
     uint32_t sparse_per_tile;  // count pass: sparse once the bracket holds <= this x tiles keys
+    // warm builds (null otherwise): per heap slot the previous tree's cut and w x its extent
+    // (x NaN: no hint) and that tree's cut axis
+    const float2 *hint;     // (cut, w x extent) from the previous tree
+    const int *hint_axis;
+    uint8_t *warm;          // [C] 1 while a hinted bracket is not yet checked
     BuildCounters *counters;
 };
 

@@ -24,7 +24,7 @@ namespace orb {
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
-    "tile_map", "bisect_warp", "bisect_tile"};
+    "tile_map", "bisect_warp", "bisect_tile", "warm_start"};
 
 namespace {
 
@@ -268,6 +268,24 @@ __global__ void k_init_batch(Level v, const BatchRoot *roots, int k) {
     }
 }
 
+// Warm builds: whether a hinted bracket [L, R) can hold the cut the bisection looks for,
+// given the counts of keys below L and below R. Outside it every tested cut would keep
+// moving the same margin: count(< L) already too high, or count(< R) still too low.
+__device__ __forceinline__ bool warm_bracket_holds(uint32_t below_L, uint32_t below_R, uint32_t n) {
+    return convergence(below_L, n) <= 0 && convergence(below_R, n) >= 0;
+}
+
+// Restart of a cell whose hinted bracket missed: the reference's own start, the cell's extent
+// along its cut axis (setCutMargin, src/cell.h:123-126).
+__device__ __forceinline__ void warm_reset(orb_cell_t &cell, float &L, float &R, BuildCounters *ctr) {
+    const int a = eff_axis(cell.cutAxis);
+    L = cell.lower[a];
+    R = cell.upper[a];
+    cell.cutMarginLeft = L;
+    cell.cutMarginRight = R;
+    atomicAdd(&ctr->warm_resets, 1u);
+}
+
 // ------------------------------------------------------------------------------------
 // Plan: per-cell tile and histogram offsets (single CTA, any C).
 // ------------------------------------------------------------------------------------
@@ -308,6 +326,42 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
         v.hist_off[C] = tot_b;
         v.ptile_off[C] = tot_p;
     }
+}
+
+// Warm builds, after the plan: a cell whose previous tree cut on the same axis starts from
+// the hinted bracket (clipped to its extent) when that narrows it. Its first count pass is
+// then sparse: most keys lie outside. One thread per cell.
+__global__ void k_warm_start(Level v) {
+    const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    uint32_t nwarm = 0;
+    if (c < v.C) {
+        const int slot = level_slot(v, c);
+        orb_cell_t &cell = v.heap[slot];
+        const uint2 rg = v.ranges[slot];
+        const uint32_t n = rg.y - rg.x;
+        const float2 h = v.hint[slot];
+        uint8_t w = 0;
+        if (n > 1 && !isnan(h.x) && v.hint_axis[slot] == cell.cutAxis && cell.cutAxis >= 0) {
+            // half-width w x extent / sqrt(n): about w sqrt(n) keys each side if evenly spread,
+            // the scale by which a median drifts when the particles move a little
+            const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+            const float half = __fdiv_rn(h.y, sqrtf((float)n));
+            const float Lw = fmaxf(L, __fsub_rn(h.x, half)), Rw = fminf(R, __fadd_rn(h.x, half));
+            if (Lw < Rw && (Lw > L || Rw < R)) {
+                cell.cutMarginLeft = Lw;
+                cell.cutMarginRight = Rw;
+                w = 1;
+                // keys in the bracket if spread evenly, capped so the first pass is sparse
+                const float share = __fdiv_rn(__fsub_rn(Rw, Lw), __fsub_rn(R, L));
+                const uint32_t tiles = (n + kTile - 1) / kTile;
+                v.inb[c] = min((uint32_t)fminf((float)n, ceilf(share * (float)n)), v.sparse_per_tile * tiles);
+                nwarm = 1;
+            }
+        }
+        v.warm[c] = w;
+    }
+    nwarm = warp_sum(nwarm);
+    if ((threadIdx.x & 31) == 0 && nwarm) atomicAdd(&v.counters->warm_cells, nwarm);
 }
 
 // ------------------------------------------------------------------------------------
@@ -439,7 +493,9 @@ __device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, 
 
 
 
-// One bracket key of a sparse pass into the cell's global bins (out of line, as above).
+// One bracket key of a sparse pass into the cell's bins (global, or shared for a sparse
+// pass whose bracket holds more than kSparseGlobalKeys keys a tile), out of line as above.
+constexpr uint32_t kSparseGlobalKeys = 8;
 __device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R, int K) {
     atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
 }
@@ -559,11 +615,15 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
         uint32_t *gh = v.hist + v.hist_off[tr.c];
         const bool sparse = v.inb[tr.c] <= v.sparse_per_tile * cell_tiles;
-        if (!sparse) {
+        // a sparse pass whose bracket still holds more than a few keys a tile bins them in
+        // shared memory first (no global atomics on the same bins from every tile)
+        const bool local = sparse && v.inb[tr.c] > kSparseGlobalKeys * cell_tiles;
+        if (!sparse || local) {
             for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) s_hist[j] = 0u;
-            fill_edges(s_edge, L, R, K, threadIdx.x, blockDim.x);
+            if (!sparse) fill_edges(s_edge, L, R, K, threadIdx.x, blockDim.x);
             __syncthreads();
         }
+        uint32_t *sbins = local ? s_hist : gh;  // where a sparse pass's bracket keys go
         const float m = bin_margin(L, R, scale, nb);
         const float one_m = __fsub_rd(1.0f, m);
         uint32_t below = 0;
@@ -575,12 +635,12 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
                     below += k < L;
                     return !(k >= L && k < R);
                 },
-                [&](float k) { add_sparse(gh, k, L, R, K); },
+                [&](float k) { add_sparse(sbins, k, L, R, K); },
                 [&](float k) {
                     if (k < L)
                         ++below;
                     else if (k < R)
-                        add_sparse(gh, k, L, R, K);
+                        add_sparse(sbins, k, L, R, K);
                 });
         } else {
             // dense: the scaled guess alone, no range test (a key below L gives a guess below
@@ -612,7 +672,7 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
             if (below) atomicAdd(&v.below[tr.c], below);
             bytes += 4ull * (tr.e1 - tr.e0);
         }
-        if (!sparse) {
+        if (!sparse || local) {
             for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
                 const uint32_t h = s_hist[b];
                 if (h) atomicAdd(&gh[b], h);
@@ -655,6 +715,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
         float L = cell.cutMarginLeft, R = cell.cutMarginRight;
         uint32_t it = 0, cand = n;
         int st = kActive;
+        bool warm = v.warm && v.warm[c];  // hinted bracket, checked by the first round
         while (st == kActive) {
             bytes += 4ull * n;
             if (cand <= kListKeys) {
@@ -733,6 +794,18 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
                 run += h;
             }
             __syncwarp();
+            if (warm) {
+                warm = false;
+                if (!warm_bracket_holds(below, below + tot, n)) {  // restart on the extent
+                    const int a = eff_axis(cell.cutAxis);
+                    L = cell.lower[a];
+                    R = cell.upper[a];
+                    cand = n;
+                    if (lane == 0) atomicAdd(&v.counters->warm_resets, 1u);
+                    __syncwarp();
+                    continue;
+                }
+            }
             // replay up to K iterations (identically in every lane)
             uint32_t pos = 0, width = nb;
             for (int step = 0; step < K; ++step) {
@@ -767,6 +840,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
             cell.foundCut = st == kFound ? 1 : 0;
             v.iters[c] = (uint8_t)it;
             v.state[c] = (uint8_t)st;
+            if (v.warm) v.warm[c] = 0;
             atomicMax(&v.counters->max_iters, it);
             if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
         }
@@ -793,6 +867,34 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     uint32_t prefix = v.below[c];
     uint32_t pos = 0, width = 1u << K;
     uint8_t st = kActive;
+    uint32_t first_half = 0xffffffffu;  // bins below the first cut, when already summed
+    if (v.warm && v.warm[c]) {
+        // first pass of a hinted bracket: check it holds the target before replaying (one
+        // sweep over the bins gives the total and the first step's count)
+        const uint32_t h0 = 1u << (K - 1);
+        uint32_t lo = 0, hi = 0;
+        for (uint32_t b = lane; b < h0; b += 32) {
+            lo += g[b];
+            hi += g[b + h0];
+        }
+        lo = warp_sum(lo);
+        hi = warp_sum(hi);
+        first_half = lo;
+        const bool holds = warm_bracket_holds(prefix, prefix + lo + hi, n);
+        __syncwarp();
+        if (!holds) {
+            for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
+            if (lane == 0) {
+                warm_reset(cell, L, R, v.counters);
+                v.warm[c] = 0;
+                v.inb[c] = n;
+                v.below[c] = 0;
+                v.counters->any_active[v.pass & 1] = 1u;
+            }
+            return;  // the next pass bins the whole extent
+        }
+        if (lane == 0) v.warm[c] = 0;
+    }
     for (int step = 0; step < K; ++step) {
         if (it >= (uint32_t)kMaxIterations) {
             st = kCapped;
@@ -800,8 +902,12 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         }
         const uint32_t half = width >> 1;
         uint32_t sum = 0;
-        for (uint32_t b = lane; b < half; b += 32) sum += g[pos + b];
-        sum = warp_sum(sum);
+        if (step == 0 && first_half != 0xffffffffu) {
+            sum = first_half;
+        } else {
+            for (uint32_t b = lane; b < half; b += 32) sum += g[pos + b];
+            sum = warp_sum(sum);
+        }
         const uint32_t cl = prefix + sum;
         ++it;
         const int dir = convergence(cl, n);
@@ -865,6 +971,22 @@ __global__ void __launch_bounds__(kThreads) k_bisect_warp(Level v) {
         k[j] = i < n ? __ldg(keys + rg.x + i) : __int_as_float(0x7fc00000);  // NaN: never below
     }
     float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    if (v.warm && v.warm[c]) {
+        // hinted bracket: keep it only if it holds the target
+        uint32_t bl = 0, br = 0;
+#pragma unroll
+        for (int j = 0; j < kWarpKeysPerLane; ++j) {
+            bl += k[j] < L;
+            br += k[j] < R;
+        }
+        if (!warm_bracket_holds(warp_sum(bl), warp_sum(br), n)) {
+            const int a = eff_axis(cell.cutAxis);
+            L = cell.lower[a];
+            R = cell.upper[a];
+            if (lane == 0) atomicAdd(&v.counters->warm_resets, 1u);
+        }
+        if (lane == 0) v.warm[c] = 0;
+    }
     uint32_t it = 0;
     uint8_t st = kActive;
     while (st == kActive) {
@@ -1725,6 +1847,7 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
         case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
+        case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
         case kKBisectCta:
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;

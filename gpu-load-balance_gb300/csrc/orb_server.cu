@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -94,6 +95,7 @@ struct Req {
     int gen_kind = 0;               // kGenerate
     uint64_t seed = 0;              // kGenerate: generator seed; kRebalance: displacement seed
     float sigma = 0.f;
+    float warm = 0.f;               // kRebalance: > 0 = warm rebuild, bracket half-width
     double t_submit = 0, t_start = 0, t_done = 0;
     orb_status status = ORB_OK;
     bool done = false;
@@ -190,8 +192,9 @@ void lane_loop(orb_server *sv, int lane) {
     cudaSetDevice(sv->device);
     orb_ctx *ctx = sv->lanes[lane].ctx;
     cudaStream_t st = orb::ctx_stream(ctx);
-    std::vector<orb_cell_t> heaps;
+    std::vector<orb_cell_t> heaps, prev;
     std::vector<uint32_t> rgs;
+    std::vector<float> widths;
     for (;;) {
         std::vector<Req *> batch;
         std::vector<Inst *> ins;  // element pointers of an unordered_map stay valid
@@ -244,9 +247,30 @@ void lane_loop(orb_server *sv, int lane) {
         heaps.resize(std::max<size_t>(heap_cells, 1));
         rgs.resize(2 * std::max<size_t>(heap_cells, 1));
         orb_build_info info;
-        if (status == ORB_OK)
+        // warm rebalances start from their instance's current tree (a labelled mode: not
+        // bit-identical with a cold rebuild); every other request of the batch builds cold
+        bool any_warm = false;
+        for (size_t i = 0; i < batch.size(); ++i)
+            any_warm |= batch[i]->kind == kRebalance && batch[i]->warm > 0.f && ins[i]->heap.size() == 2ull * ins[i]->d - 1;
+        if (status == ORB_OK && any_warm) {
+            prev.assign(std::max<size_t>(heap_cells, 1), orb_cell_t{});
+            widths.assign(batch.size(), 0.f);
+            size_t hb = 0;
+            for (size_t i = 0; i < batch.size(); ++i) {
+                const size_t hc = 2ull * ins[i]->d - 1;
+                if (batch[i]->kind == kRebalance && batch[i]->warm > 0.f && ins[i]->heap.size() == hc) {
+                    std::copy(ins[i]->heap.begin(), ins[i]->heap.end(), prev.begin() + hb);
+                    widths[i] = batch[i]->warm;
+                }
+                hb += hc;
+            }
+            status = orb_build_batch_warm(ctx, sv->ax, sv->ay, sv->az, sv->arena_cap, desc.data(),
+                                          (uint32_t)desc.size(), prev.data(), widths.data(), heaps.data(),
+                                          rgs.data(), sv->aperm, ORB_DEVICE_POINTERS, &info);
+        } else if (status == ORB_OK) {
             status = orb_build_batch(ctx, sv->ax, sv->ay, sv->az, sv->arena_cap, desc.data(), (uint32_t)desc.size(),
                                      heaps.data(), rgs.data(), sv->aperm, ORB_DEVICE_POINTERS, &info);
+        }
         if (status == ORB_OK) {
             // original index of every particle: ident <- ident[perm] per instance
             for (const orb_batch_instance &b : desc) {
@@ -434,9 +458,9 @@ orb_status orb_server_submit_generate(orb_server *sv, int kind, uint64_t seed, u
     return new_instance(sv, n, d, levels, nullptr, nullptr, r, request_id);
 }
 
-orb_status orb_server_submit_rebalance(orb_server *sv, uint64_t instance_id, uint64_t seed, float sigma,
-                                       uint64_t *request_id) {
-    if (!sv || !(sigma >= 0.f)) return ORB_ERR_INVALID_ARGUMENT;
+static orb_status submit_rebalance(orb_server *sv, uint64_t instance_id, uint64_t seed, float sigma,
+                                   float warm, uint64_t *request_id) {
+    if (!sv || !(sigma >= 0.f) || !(warm >= 0.f) || !std::isfinite(warm)) return ORB_ERR_INVALID_ARGUMENT;
     {
         std::lock_guard<std::mutex> lk(sv->mu);
         auto it = sv->insts.find(instance_id);
@@ -447,7 +471,19 @@ orb_status orb_server_submit_rebalance(orb_server *sv, uint64_t instance_id, uin
     r->inst = instance_id;
     r->seed = seed;
     r->sigma = sigma;
+    r->warm = warm;
     return submit(sv, std::move(r), request_id);
+}
+
+orb_status orb_server_submit_rebalance(orb_server *sv, uint64_t instance_id, uint64_t seed, float sigma,
+                                       uint64_t *request_id) {
+    return submit_rebalance(sv, instance_id, seed, sigma, 0.f, request_id);
+}
+
+orb_status orb_server_submit_rebalance_warm(orb_server *sv, uint64_t instance_id, uint64_t seed,
+                                            float sigma, float width, uint64_t *request_id) {
+    if (!(width > 0.f)) return ORB_ERR_INVALID_ARGUMENT;
+    return submit_rebalance(sv, instance_id, seed, sigma, width, request_id);
 }
 
 orb_status orb_server_wait(orb_server *sv, uint64_t request_id, orb_request_result *out) {

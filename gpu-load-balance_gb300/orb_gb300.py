@@ -66,7 +66,8 @@ EXPORTS = [
     "orb_profile_kernel_index", "orb_server_create", "orb_server_destroy", "orb_server_submit_build",
     "orb_server_submit_generate", "orb_server_submit_rebalance", "orb_server_wait", "orb_server_poll",
     "orb_server_fetch", "orb_server_release", "orb_server_get_stats", "orb_get_tuning",
-    "orb_set_tuning", "orb_autotune_batch",
+    "orb_set_tuning", "orb_autotune_batch", "orb_build_batch_warm", "orb_build_warm",
+    "orb_server_submit_rebalance_warm",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -146,6 +147,8 @@ class BuildInfo(ctypes.Structure):
         ("device_ms", ctypes.c_float),
         ("h2d_ms", ctypes.c_float),
         ("d2h_ms", ctypes.c_float),
+        ("warm_cells", ctypes.c_uint32),
+        ("warm_resets", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -258,6 +261,15 @@ def load(path: str | None = None):
     L.orb_server_submit_build.argtypes = [vp, vp, vp, vp, u64, u32, u32, vp, vp, ctypes.POINTER(u64)]
     L.orb_server_submit_generate.restype = ctypes.c_int
     L.orb_server_submit_generate.argtypes = [vp, ctypes.c_int, u64, u64, u32, u32, ctypes.POINTER(u64)]
+    L.orb_server_submit_rebalance_warm.restype = ctypes.c_int
+    L.orb_server_submit_rebalance_warm.argtypes = [vp, u64, u64, ctypes.c_float, ctypes.c_float,
+                                                   ctypes.POINTER(u64)]
+    L.orb_build_warm.restype = ctypes.c_int
+    L.orb_build_warm.argtypes = [vp, vp, vp, vp, u64, u32, u32, vp, vp, vp, ctypes.c_float, vp, vp, vp,
+                                 u32, ctypes.POINTER(BuildInfo)]
+    L.orb_build_batch_warm.restype = ctypes.c_int
+    L.orb_build_batch_warm.argtypes = [vp, vp, vp, vp, u64, ctypes.POINTER(BatchInstance), u32, vp, vp,
+                                       vp, vp, vp, u32, ctypes.POINTER(BuildInfo)]
     L.orb_server_submit_rebalance.restype = ctypes.c_int
     L.orb_server_submit_rebalance.argtypes = [vp, u64, u64, ctypes.c_float, ctypes.POINTER(u64)]
     L.orb_server_wait.restype = ctypes.c_int
@@ -355,6 +367,53 @@ class Context:
                                 ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
         self._check(st)
         return BuildResult(heap, ranges, perm, info.as_dict())
+
+    def build_warm(self, x, y, z, d: int, prev_heap, width: float, levels: int = 0,
+                   lower=(-0.5, -0.5, -0.5), upper=(0.5, 0.5, 0.5), perm=True,
+                   device_pointers: bool = False) -> BuildResult:
+        """Warm-started build from a previous tree (orb_build_warm): a valid ORB tree, not
+        bit-identical with build() on the same particles."""
+        n = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        heap = np.zeros(2 * d - 1, CELL_DTYPE)
+        ranges = np.zeros((2 * d - 1, 2), np.uint32)
+        prev = np.ascontiguousarray(prev_heap, dtype=CELL_DTYPE)
+        if perm is True:
+            perm = np.empty(n, np.uint32)
+        lo = np.asarray(lower, np.float32)
+        hi = np.asarray(upper, np.float32)
+        info = BuildInfo()
+        st = self.lib.orb_build_warm(self.h, _ptr(x), _ptr(y), _ptr(z), n, d, levels, lo.ctypes.data,
+                                     hi.ctypes.data, prev.ctypes.data, width, heap.ctypes.data,
+                                     ranges.ctypes.data, _ptr(perm),
+                                     ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
+        self._check(st)
+        return BuildResult(heap, ranges, perm, info.as_dict())
+
+    def build_batch_warm(self, x, y, z, instances, prev_heaps, widths, perm=True,
+                         device_pointers: bool = False):
+        """Warm-started batched build (orb_build_batch_warm); prev_heaps laid out like the
+        heaps build_batch returns back to back, widths one per instance (0 = cold)."""
+        k = len(instances)
+        arr, heap_cells, bases = self._instances(instances)
+        n_total = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        heaps = np.zeros(max(heap_cells, 1), CELL_DTYPE)
+        ranges = np.zeros((max(heap_cells, 1), 2), np.uint32)
+        prev = np.ascontiguousarray(prev_heaps, dtype=CELL_DTYPE)
+        w = np.ascontiguousarray(widths, dtype=np.float32)
+        if perm is True:
+            perm = np.empty(n_total, np.uint32)
+        info = BuildInfo()
+        st = self.lib.orb_build_batch_warm(self.h, _ptr(x), _ptr(y), _ptr(z), n_total, arr, k,
+                                           prev.ctypes.data, w.ctypes.data, heaps.ctypes.data,
+                                           ranges.ctypes.data, _ptr(perm),
+                                           ORB_DEVICE_POINTERS if device_pointers else 0,
+                                           ctypes.byref(info))
+        self._check(st)
+        parts = []
+        for i, ins in enumerate(instances):
+            hc = 2 * int(ins["d"]) - 1
+            parts.append((heaps[bases[i]:bases[i] + hc], ranges[bases[i]:bases[i] + hc]))
+        return parts, heaps, perm, info.as_dict()
 
     @staticmethod
     def _instances(instances):
@@ -543,10 +602,16 @@ class Server:
         self.d[rid.value] = (d, n)
         return rid.value
 
-    def submit_rebalance(self, instance: int, seed: int, sigma: float) -> int:
+    def submit_rebalance(self, instance: int, seed: int, sigma: float, warm: float = 0.0) -> int:
+        """Rebalance: displace and rebuild. warm > 0 selects the warm-started rebuild with
+        that bracket factor (orb_build_batch_warm; not bit-identical with a cold one)."""
         rid = ctypes.c_uint64()
-        self._chk(self.lib.orb_server_submit_rebalance(self.h, instance, seed, sigma,
-                                                       ctypes.byref(rid)), "submit_rebalance")
+        if warm > 0:
+            st = self.lib.orb_server_submit_rebalance_warm(self.h, instance, seed, sigma, warm,
+                                                           ctypes.byref(rid))
+        else:
+            st = self.lib.orb_server_submit_rebalance(self.h, instance, seed, sigma, ctypes.byref(rid))
+        self._chk(st, "submit_rebalance")
         return rid.value
 
     def wait(self, request: int) -> dict:

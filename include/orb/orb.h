@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define ORB_ABI_VERSION 1
+#define ORB_ABI_VERSION 2
 
 typedef enum orb_status {
     ORB_OK = 0,
@@ -87,6 +87,8 @@ typedef struct orb_build_info {
     float device_ms;            /* device time of the build (CUDA events on the ctx stream) */
     float h2d_ms;               /* host->device copy time (host-pointer calls) */
     float d2h_ms;               /* device->host copy time (host-pointer calls) */
+    uint32_t warm_cells;        /* warm builds: cells that started from a hinted bracket */
+    uint32_t warm_resets;       /* ... whose hinted bracket missed the target and restarted */
 } orb_build_info;
 
 /* Context lifetime. device = CUDA ordinal. opts may be NULL. */
@@ -141,6 +143,32 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
                            const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
                            uint32_t *ranges, uint32_t *perm, uint32_t flags,
                            orb_build_info *info);
+
+/*
+ * Warm-started builds (no counterpart in the reference; the thesis's improved root finding,
+ * notes.tex:2565, and the unused FAST_MEDIAN branch, src/orbit.cpp:214-227, point at it).
+ * For rebuilding a tree after small particle moves: each cell's bisection starts from the
+ * previous tree's cut of the same cell +- width x that cell's extent / sqrt(n) (n = the new
+ * cell's particles: about width x sqrt(n) keys on each side when evenly spread, the scale by
+ * which a median drifts under small independent moves), clipped to the new cell, when the
+ * cut axis is unchanged, instead of the cell's whole extent. The bracket is
+ * checked on the first count; one that does not hold the target restarts from the extent.
+ * Every cut still passes the reference's convergence test (or the 32-sweep cap), but the
+ * midpoint sequence differs from a cold build, so the tree is NOT bit-identical with
+ * orb_build on the same particles: a separate, labelled mode.
+ *   prev_heaps: the previous trees, laid out like heaps (instance i at sum_{j<i}(2 d_j - 1));
+ *   widths[i]:  instance i's bracket factor (above; 8 is a good start), 0 = cold build.
+ */
+orb_status orb_build_batch_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
+                                const orb_batch_instance *inst, uint32_t k,
+                                const orb_cell_t *prev_heaps, const float *widths,
+                                orb_cell_t *heaps, uint32_t *ranges, uint32_t *perm,
+                                uint32_t flags, orb_build_info *info);
+orb_status orb_build_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                          uint32_t levels, const float lower[3], const float upper[3],
+                          const orb_cell_t *prev_heap, float width, orb_cell_t *heap_out,
+                          uint32_t *ranges_out, uint32_t *perm, uint32_t flags,
+                          orb_build_info *info);
 
 /*
  * Launch tuning of a context (no counterpart in the reference). Every parameter changes
@@ -224,6 +252,11 @@ orb_status orb_server_submit_generate(orb_server *sv, int kind, uint64_t seed, u
    instance's box, then the tree is rebuilt with the reference's rule. */
 orb_status orb_server_submit_rebalance(orb_server *sv, uint64_t instance_id, uint64_t seed,
                                        float sigma, uint64_t *request_id);
+/* Warm rebalance: as above, but the rebuild starts every cell from the instance's previous
+ * cut (orb_build_batch_warm with this width factor); not bit-identical with a cold rebuild.
+ * width > 0. */
+orb_status orb_server_submit_rebalance_warm(orb_server *sv, uint64_t instance_id, uint64_t seed,
+                                            float sigma, float width, uint64_t *request_id);
 /* Blocks until the request finishes; returns its status. */
 orb_status orb_server_wait(orb_server *sv, uint64_t request_id, orb_request_result *out);
 /* Finished requests not yet polled (up to max). */

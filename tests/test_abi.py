@@ -35,7 +35,7 @@ def test_library_is_sm103a(engine):
 
 def test_status_strings(engine):
     lib = engine.load()
-    assert lib.orb_abi_version() == 1
+    assert lib.orb_abi_version() == 2
     for code, text in engine.STATUS.items():
         assert lib.orb_status_string(code).decode() == text
 
