@@ -74,7 +74,9 @@ struct orb_ctx {
     DevBuf<uint32_t> htile_cell, ptile_cell;
     // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
     orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u};
-    DevBuf<uint8_t> hist_k, state, iters;
+    DevBuf<uint8_t> hist_k, state, iters, listed, cmp_bad;
+    DevBuf<uint32_t> cmp_off, cmp_cnt;
+    DevBuf<float> cmp_keys;
     DevBuf<uint32_t> hist;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
     DevBuf<unsigned long long> pt_status;
@@ -180,6 +182,12 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->hist_k.ensure(max_cells));
     ORB_CUDA(ctx->state.ensure(max_cells));
     ORB_CUDA(ctx->iters.ensure(max_cells));
+    ORB_CUDA(ctx->listed.ensure(max_cells));
+    ORB_CUDA(ctx->cmp_bad.ensure(max_cells));
+    ORB_CUDA(ctx->cmp_off.ensure(max_cells + 1));
+    ORB_CUDA(ctx->cmp_cnt.ensure(max_cells));
+    // compaction lists: n/16 per cell of more than one tile, at least 2048 (list_capacity)
+    ORB_CUDA(ctx->cmp_keys.ensure(n / 16 + 2048ull * (n / kTile + 1) + 16));
     ORB_CUDA(ctx->slots.ensure(max_cells));
     ORB_CUDA(ctx->hist.ensure(max_bins, true));
     ORB_CUDA(ctx->ptile_off.ensure(max_cells + 1));
@@ -204,6 +212,11 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.hist_k = ctx->hist_k.p;
     v.state = ctx->state.p;
     v.iters = ctx->iters.p;
+    v.listed = ctx->listed.p;
+    v.cmp_bad = ctx->cmp_bad.p;
+    v.cmp_off = ctx->cmp_off.p;
+    v.cmp_cnt = ctx->cmp_cnt.p;
+    v.cmp_keys = ctx->cmp_keys.p;
     v.hist = ctx->hist.p;
     v.below = ctx->below.p;
     v.inb = ctx->inb.p;
@@ -371,6 +384,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.heap, (const void *)v.ranges, (const void *)v.tile_off,
                           (const void *)v.hist_off, (const void *)v.hist_k, (const void *)v.state,
                           (const void *)v.iters, (const void *)v.hist, (const void *)v.below,
+                          (const void *)v.listed, (const void *)v.cmp_keys, (const void *)v.cmp_off,
                           (const void *)v.inb, (const void *)v.htile_cell,
                           (const void *)v.ptile_cell, (const void *)v.ptile_off, (const void *)v.ge_bits,
                           (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
@@ -429,8 +443,8 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         v.C = d.C;
         if (v.C == 0) continue;
         run_kernel(ctx, kKPlan, v, 1);
-        if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
+        if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
         if (ctx->tune.cta_min_cells && !v.hint && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
             // many cells: one CTA bisects one cell, no host round trip
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
@@ -554,6 +568,8 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
         ctx->tune_work[a].release();
     }
     ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release();
+    ctx->listed.release(); ctx->cmp_bad.release(); ctx->cmp_off.release(); ctx->cmp_cnt.release();
+    ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     collect_profile(ctx);
     drop_all_graphs(ctx);
@@ -1202,9 +1218,9 @@ orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out) {
 }
 
 static bool tuning_valid(const orb_tuning &t) {
-    return t.hist_blocks_per_sm >= 1 && t.hist_blocks_per_sm <= (uint32_t)kHistBlocksPerSm &&
+    return t.hist_blocks_per_sm >= 1 && t.hist_blocks_per_sm <= 8 &&
            t.part_blocks_per_sm >= 1 && t.part_blocks_per_sm <= 16 && t.tile_blocks_per_sm >= 1 &&
-           t.tile_blocks_per_sm <= (uint32_t)kTileBlocksPerSm && t.sparse_keys_per_tile >= 1 &&
+           t.tile_blocks_per_sm <= 8 && t.sparse_keys_per_tile >= 1 &&
            t.sparse_keys_per_tile <= (uint32_t)kTile;
 }
 

@@ -85,6 +85,13 @@ struct Level {
     uint32_t *hist;         // histogram pool (kept all-zero between passes)
     uint32_t *below;        // [C]   keys below the left margin in the current pass
     uint32_t *inb;          // [C]   keys inside the current bracket (n before the first pass)
+    // in-bracket compaction: a sparse pass also writes its bracket keys to the cell's list;
+    // every later pass of the cell reads the list only (count below L carried by resolve)
+    uint32_t *cmp_off;      // [C+1] first list slot of each cell (capacity = difference)
+    uint32_t *cmp_cnt;      // [C]   keys written to the list
+    float *cmp_keys;        // the lists
+    uint8_t *listed;        // [C]   1: this pass reads the cell's list instead of its keys
+    uint8_t *cmp_bad;       // [C]   1: a tile's bracket keys overflowed (no list)
     // partition
     uint32_t *ptile_off;    // [C+1] first partition tile of each cell
     uint32_t *ge_bits;      // [ptiles * kPWords] bit p: key >= cut

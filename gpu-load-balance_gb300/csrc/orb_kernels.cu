@@ -198,6 +198,12 @@ __device__ __forceinline__ TileRef tile_ref(const Level &v, uint32_t t) {
     return r;
 }
 
+// Capacity of a cell's compaction list: cells the histogram passes bisect (more than one
+// tile) get n/16 keys, at least 2048 (16x the sparse threshold's bracket).
+__host__ __device__ __forceinline__ uint32_t list_capacity(uint32_t n) {
+    return n > (uint32_t)kTile ? (n / 16 > 2048u ? n / 16 : 2048u) : 0u;
+}
+
 __device__ __forceinline__ int tree_depth(uint32_t n) {
     int lg = 31 - __clz(max(n, 1u));  // floor(log2 n)
     return max(4, min(kMaxBinsLog2, lg - 1));
@@ -294,37 +300,36 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
     const int C = v.C, tid = threadIdx.x, nt = blockDim.x;
     const int per = (C + nt - 1) / nt;
     const int c0 = min(C, tid * per), c1 = min(C, c0 + per);
-    uint32_t ta = 0, tb = 0, tp = 0;
+    uint32_t ta = 0, tb = 0, tp = 0, tc = 0;
     for (int c = c0; c < c1; ++c) {
         const uint2 rg = v.ranges[level_slot(v, c)];
         const uint32_t n = rg.y - rg.x;
         ta += (n + kTile - 1) / kTile;
         tb += 1u << tree_depth(n);
         tp += (n + kPTile - 1) / kPTile;
+        tc += list_capacity(n);
     }
-    uint32_t tot_a, tot_b, tot_p, unused;
+    uint32_t tot_a, tot_b, tot_p, tot_c;
     uint2 p = block_excl_scan2(ta, tb, sh, &tot_a, &tot_b);
-    uint32_t pp = block_excl_scan2(tp, 0u, sh, &tot_p, &unused).x;
+    const uint2 pc = block_excl_scan2(tp, tc, sh, &tot_p, &tot_c);
+    uint32_t pp = pc.x, cc = pc.y;
     for (int c = c0; c < c1; ++c) {
         const uint2 rg = v.ranges[level_slot(v, c)];
         const uint32_t n = rg.y - rg.x;
-        const int k = tree_depth(n);
         v.tile_off[c] = p.x;
         v.hist_off[c] = p.y;
         v.ptile_off[c] = pp;
+        v.cmp_off[c] = cc;
         pp += (n + kPTile - 1) / kPTile;
-        v.hist_k[c] = (uint8_t)k;
-        v.state[c] = n <= (uint32_t)kWarpKeys ? kSmall : (n <= (uint32_t)kTile ? kOneTile : kActive);
-        v.iters[c] = 0;
-        v.below[c] = 0;
-        v.inb[c] = n;
+        cc += list_capacity(n);
         p.x += (n + kTile - 1) / kTile;
-        p.y += 1u << k;
+        p.y += 1u << tree_depth(n);
     }
     if (tid == 0) {
         v.tile_off[C] = tot_a;
         v.hist_off[C] = tot_b;
         v.ptile_off[C] = tot_p;
+        v.cmp_off[C] = tot_c;
     }
 }
 
@@ -496,6 +501,53 @@ __device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, 
 // One bracket key of a sparse pass into the cell's bins (global, or shared for a sparse
 // pass whose bracket holds more than kSparseGlobalKeys keys a tile), out of line as above.
 constexpr uint32_t kSparseGlobalKeys = 8;
+constexpr int kCmpTile = 1024;  // bracket keys a tile can compact (more: the cell keeps no list)
+
+// Count pass over a cell whose bracket keys an earlier pass compacted: tile j of the cell
+// takes list keys [j kTile, (j+1) kTile) and bins those inside [L, R) (the keys below L are
+// already counted: resolve carried them). Returns the keys read. Out of line: the streaming
+// loop's registers stay its own.
+__device__ __noinline__ uint32_t listed_tile(const Level &v, const TileRef &tr, float L, float R,
+                                             int K, uint32_t *gh) {
+    const uint32_t cnt = v.cmp_cnt[tr.c];
+    const uint32_t lo = tr.local * (uint32_t)kTile, hi = min(cnt, lo + (uint32_t)kTile);
+    const float *list = v.cmp_keys + v.cmp_off[tr.c];
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float k = list[i];
+        if (k >= L && k < R) atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
+    }
+    return hi > lo ? hi - lo : 0u;
+}
+
+// Appends a sparse tile's compacted bracket keys (nk of them in s_cmp) to its cell's list:
+// one reservation per tile; an overflow (of the tile's buffer or the list) marks the cell
+// as having no list. Returns the keys written. Every thread of the CTA calls it.
+__device__ __noinline__ uint32_t append_list(const Level &v, int c, const float *s_cmp, uint32_t nk,
+                                             uint32_t *s_base) {
+    if (threadIdx.x == 0) {
+        const uint32_t cap = v.cmp_off[c + 1] - v.cmp_off[c];
+        *s_base = 0xffffffffu;
+        if (nk > (uint32_t)kCmpTile) {
+            v.cmp_bad[c] = 1;
+        } else if (nk) {
+            const uint32_t b = atomicAdd(&v.cmp_cnt[c], nk);
+            if (b + nk > cap)
+                v.cmp_bad[c] = 1;
+            else
+                *s_base = b;
+        }
+    }
+    __syncthreads();
+    const uint32_t b = *s_base;
+    uint32_t wrote = 0;
+    if (b != 0xffffffffu) {
+        float *list = v.cmp_keys + v.cmp_off[c] + b;
+        for (uint32_t i = threadIdx.x; i < nk; i += blockDim.x) list[i] = s_cmp[i];
+        wrote = nk;
+    }
+    __syncthreads();  // s_cmp and the count are reused by the next tile
+    return wrote;
+}
 __device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R, int K) {
     atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
 }
@@ -597,6 +649,8 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
     __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
+    __shared__ float s_cmp[kCmpTile];  // a sparse tile's bracket keys, on their way to the list
+    __shared__ uint32_t s_ncmp, s_base;
     if (blockIdx.x == 0 && threadIdx.x == 0) v.counters->any_active[v.pass & 1] = 0u;
     // every cell of the level finished in an earlier pass: nothing to bin
     if (v.pass > 0 && *(volatile uint32_t *)&v.counters->any_active[(v.pass - 1) & 1] == 0u) return;
@@ -612,8 +666,13 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         const int K = v.hist_k[tr.c];
         const uint32_t nb = 1u << K;
         const int top = (int)nb - 1;
-        const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
         uint32_t *gh = v.hist + v.hist_off[tr.c];
+        if (v.listed[tr.c]) {
+            const uint32_t nread = listed_tile(v, tr, L, R, K, gh);
+            if (threadIdx.x == 0) bytes += 4ull * nread;
+            continue;
+        }
+        const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
         const bool sparse = v.inb[tr.c] <= v.sparse_per_tile * cell_tiles;
         // a sparse pass whose bracket still holds more than a few keys a tile bins them in
         // shared memory first (no global atomics on the same bins from every tile)
@@ -624,6 +683,18 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
             __syncthreads();
         }
         uint32_t *sbins = local ? s_hist : gh;  // where a sparse pass's bracket keys go
+        // ... and compacted into the cell's list when the bracket after this pass is still
+        // expected to hold more than a few keys a bin (so a further pass will follow)
+        const bool compact = sparse && v.inb[tr.c] > (8u << K);
+        if (compact) {
+            if (threadIdx.x == 0) s_ncmp = 0;
+            __syncthreads();
+        }
+        auto keep = [&](float k) {
+            if (!compact) return;
+            const uint32_t i = atomicAdd(&s_ncmp, 1u);
+            if (i < (uint32_t)kCmpTile) s_cmp[i] = k;
+        };
         const float m = bin_margin(L, R, scale, nb);
         const float one_m = __fsub_rd(1.0f, m);
         uint32_t below = 0;
@@ -635,12 +706,17 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
                     below += k < L;
                     return !(k >= L && k < R);
                 },
-                [&](float k) { add_sparse(sbins, k, L, R, K); },
                 [&](float k) {
-                    if (k < L)
+                    add_sparse(sbins, k, L, R, K);
+                    keep(k);
+                },
+                [&](float k) {
+                    if (k < L) {
                         ++below;
-                    else if (k < R)
+                    } else if (k < R) {
                         add_sparse(sbins, k, L, R, K);
+                        keep(k);
+                    }
                 });
         } else {
             // dense: the scaled guess alone, no range test (a key below L gives a guess below
@@ -671,6 +747,10 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         if (threadIdx.x == 0) {
             if (below) atomicAdd(&v.below[tr.c], below);
             bytes += 4ull * (tr.e1 - tr.e0);
+        }
+        if (compact) {
+            const uint32_t wrote = append_list(v, tr.c, s_cmp, s_ncmp, &s_base);
+            if (threadIdx.x == 0) bytes += 4ull * wrote;
         }
         if (!sparse || local) {
             for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -889,6 +969,9 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
                 v.warm[c] = 0;
                 v.inb[c] = n;
                 v.below[c] = 0;
+                v.listed[c] = 0;
+                v.cmp_cnt[c] = 0;
+                v.cmp_bad[c] = 0;
                 v.counters->any_active[v.pass & 1] = 1u;
             }
             return;  // the next pass bins the whole extent
@@ -927,9 +1010,17 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     }
     if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
     const uint32_t next_inb = g[pos];  // keys in the bracket the next pass would bin
+    // the next pass reads the cell's list when this pass read one or wrote a complete one
+    // (a sparse pass compacts its bracket keys); then the keys below the new L are known
+    const uint32_t tiles = v.tile_off[c + 1] - v.tile_off[c];
+    const bool list_next = v.listed[c] || (v.inb[c] <= v.sparse_per_tile * tiles &&
+                                           v.inb[c] > (8u << K) && !v.cmp_bad[c]);
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
-    if (st == kActive && lane == 0) v.inb[c] = next_inb;
+    if (st == kActive && lane == 0) {
+        v.inb[c] = next_inb;
+        v.listed[c] = list_next ? 1 : 0;
+    }
     if (lane == 0) {
         add_bytes(v, kKResolve, 8ull << K);  // bins read and cleared
         cell.cutMarginLeft = L;
@@ -937,7 +1028,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         cell.foundCut = st == kFound ? 1 : 0;
         v.iters[c] = (uint8_t)it;
         v.state[c] = st;
-        v.below[c] = 0;
+        v.below[c] = st == kActive && list_next ? prefix : 0u;
         atomicMax(&v.counters->max_iters, it);
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
         if (st == kActive) {
@@ -1189,11 +1280,25 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
 }
 
 // Tile -> cell maps of the level (one binary search per tile, once per level).
+// ... and the per-cell state of the level, in parallel (the plan only computes the offsets).
 __global__ void k_tile_map(Level v) {
-    const uint32_t ht = v.tile_off[v.C], pt = v.ptile_off[v.C];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < max(ht, pt); t += gridDim.x * blockDim.x) {
+    const uint32_t ht = v.tile_off[v.C], pt = v.ptile_off[v.C], C = (uint32_t)v.C;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < max(max(ht, pt), C);
+         t += gridDim.x * blockDim.x) {
         if (t < ht) v.htile_cell[t] = find_cell(v.tile_off, v.C, t);
         if (t < pt) v.ptile_cell[t] = find_cell(v.ptile_off, v.C, t);
+        if (t < C) {
+            const uint2 rg = v.ranges[level_slot(v, (int)t)];
+            const uint32_t n = rg.y - rg.x;
+            v.hist_k[t] = (uint8_t)tree_depth(n);
+            v.state[t] = n <= (uint32_t)kWarpKeys ? kSmall : (n <= (uint32_t)kTile ? kOneTile : kActive);
+            v.iters[t] = 0;
+            v.below[t] = 0;
+            v.inb[t] = n;
+            v.cmp_cnt[t] = 0;
+            v.listed[t] = 0;
+            v.cmp_bad[t] = 0;
+        }
     }
 }
 

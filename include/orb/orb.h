@@ -178,7 +178,7 @@ orb_status orb_build_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n
 typedef struct orb_tuning {
     uint32_t hist_blocks_per_sm;   /* count-left pass: CTAs per SM, 1..8 (default 8) */
     uint32_t part_blocks_per_sm;   /* partition passes: CTAs per SM, 1..16 (default 8) */
-    uint32_t tile_blocks_per_sm;   /* one-tile cell bisection: CTAs per SM, 1..4 (default 4) */
+    uint32_t tile_blocks_per_sm;   /* one-tile cell bisection: CTAs per SM, 1..8 (default 4) */
     uint32_t sparse_keys_per_tile; /* compaction threshold: a count pass sends a cell's bracket
                                       keys straight to its global bins (instead of binning all
                                       keys in shared memory) once the bracket holds at most

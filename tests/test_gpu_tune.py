@@ -33,7 +33,7 @@ def test_get_set_roundtrip_and_limits(fresh, engine):
     assert fresh.get_tuning()["part_blocks_per_sm"] == 12
     assert fresh.get_tuning()["sparse_keys_per_tile"] == 100
     for bad in (dict(hist_blocks_per_sm=0), dict(hist_blocks_per_sm=9), dict(part_blocks_per_sm=17),
-                dict(tile_blocks_per_sm=5), dict(sparse_keys_per_tile=0),
+                dict(tile_blocks_per_sm=9), dict(sparse_keys_per_tile=0),
                 dict(sparse_keys_per_tile=16385)):
         with pytest.raises(engine.OrbError):
             fresh.set_tuning(**bad)
