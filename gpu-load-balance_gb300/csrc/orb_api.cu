@@ -89,6 +89,7 @@ struct orb_ctx {
     DevBuf<float2> hint;      // warm builds: starting bracket per heap slot
     DevBuf<int> hint_axis;
     DevBuf<uint8_t> warm;
+    DevBuf<uint32_t> sub_flag;  // subtree path taken (one word)
     BuildCounters *h_counters = nullptr;  // pinned
 
     // service layer state
@@ -436,12 +437,23 @@ struct LevelDesc {
 // The reference's level loop (src/orbit.cpp:102-275) over every cell of every level: plan,
 // bisection (one warp for small cells, one CTA per cell or the multi-CTA histogram passes
 // for the rest), partition and split.
-orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes) {
-    for (const LevelDesc &d : lv) {
+// sub_from >= 0: from level lv[sub_from] down, one CTA per cell finishes the tree when every
+// cell of that level fits one (k_subtree_check decides on the device); the level kernels of
+// those levels then return at once.
+orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes,
+                      int sub_from = -1) {
+    for (size_t li = 0; li < lv.size(); ++li) {
+        const LevelDesc &d = lv[li];
         v.base = d.base;
         v.slots = d.slots;
         v.C = d.C;
         if (v.C == 0) continue;
+        if ((int)li == sub_from) {
+            v.skip = ctx->sub_flag.p;
+            run_kernel(ctx, kKSubtreeCheck, v, 1, (int)(lv.size() - li));
+            run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm),
+                       (int)(lv.size() - li));
+        }
         run_kernel(ctx, kKPlan, v, 1);
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
         if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
@@ -567,7 +579,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
         ctx->tune_src[a].release();
         ctx->tune_work[a].release();
     }
-    ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release();
+    ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release(); ctx->sub_flag.release();
     ctx->listed.release(); ctx->cmp_bad.release(); ctx->cmp_off.release(); ctx->cmp_cnt.release();
     ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -641,12 +653,26 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         key_add_f(key, lower[a]);
         key_add_f(key, upper[a]);
     }
+    // subtrees from the first level whose cells (about n / 2^l, each split moving a cell's
+    // count by at most a few particles from half) all fit one CTA, once there are enough
+    // cells to fill the GPU
+    int sub_from = -1;
+    for (size_t li = 0; li < lv.size(); ++li) {
+        const uint64_t expect = (n >> li) + 1 + 8ull * li;
+        if (expect <= kSubMaxParticles && (uint64_t)lv[li].C >= 2ull * ctx->num_sms &&
+            lv.size() - li <= (size_t)kSubMaxLevels) {
+            sub_from = (int)li;
+            break;
+        }
+    }
+    if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
+    key.push_back((uint64_t)(int64_t)sub_from);
     uint32_t passes = 0;
     st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
         ctx->launches[kKInit] += 1;
         launch_init(v, n, lower, upper, d, (int)heap_cells, s);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp);
+        return run_levels(ctx, v, lv, pp, sub_from);
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));

@@ -22,6 +22,9 @@ constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
 constexpr int kHistBlocksPerSm = 8;  // resident CTAs of the count-left pass (most useful grid)
 constexpr int kTileBlocksPerSm = 4;  // resident CTAs of the one-tile cell bisection
+constexpr int kSubtreeBlocksPerSm = 4;  // CTAs of the subtree kernel per SM (its grid)
+constexpr uint32_t kSubMaxParticles = 17408;  // largest cell one subtree CTA takes
+constexpr int kSubMaxLevels = 6;              // deepest tree one subtree CTA finishes
 
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
@@ -45,8 +48,11 @@ enum Kernel : int {
     kKBisectWarp,
     kKBisectTile,
     kKWarmStart,
+    kKSubtreeCheck,
+    kKSubtree,
     kNumKernels
 };
+static_assert(kNumKernels <= 32, "BuildCounters::bytes holds 32 kernel kinds");
 extern const char *const kKernelNames[kNumKernels];
 
 // Device-side counters of one build (read back at the end).
@@ -60,7 +66,7 @@ struct BuildCounters {
     uint32_t ticket;      // block ticket of the tile scan (reset before each launch)
     uint32_t warm_cells;  // warm builds: cells that started from a hinted bracket
     uint32_t warm_resets; // ... whose hinted bracket missed the target (restarted cold)
-    unsigned long long bytes[16];  // algorithmic bytes per Kernel kind
+    unsigned long long bytes[32];  // algorithmic bytes per Kernel kind
 };
 
 // Everything a level's kernels need. Cells of the level are heap slots [base, base + C)
@@ -112,6 +118,9 @@ struct Level {
     const float2 *hint;     // (cut, w x extent) from the previous tree
     const int *hint_axis;
     uint8_t *warm;          // [C] 1 while a hinted bracket is not yet checked
+    // subtrees: 1 when one CTA per cell finishes the tree from this level down (then the
+    // level kernels of the levels below return at once); null when not attempted
+    uint32_t *skip;
     BuildCounters *counters;
 };
 

@@ -24,7 +24,7 @@ namespace orb {
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
-    "tile_map", "bisect_warp", "bisect_tile", "warm_start"};
+    "tile_map", "bisect_warp", "bisect_tile", "warm_start", "subtree_check", "subtree"};
 
 namespace {
 
@@ -296,6 +296,7 @@ __device__ __forceinline__ void warm_reset(orb_cell_t &cell, float &L, float &R,
 // Plan: per-cell tile and histogram offsets (single CTA, any C).
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_plan(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t sh[96];
     const int C = v.C, tid = threadIdx.x, nt = blockDim.x;
     const int per = (C + nt - 1) / nt;
@@ -337,6 +338,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
 // the hinted bracket (clipped to its extent) when that narrows it. Its first count pass is
 // then sparse: most keys lie outside. One thread per cell.
 __global__ void k_warm_start(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     uint32_t nwarm = 0;
     if (c < v.C) {
@@ -613,12 +615,16 @@ __device__ __forceinline__ auto each(Visit &visit) {
 // head to 16-byte alignment and scalar tail through visit(k), float4 body (kHistVec loads
 // in flight a thread) through group(k[kGroup]). `pad` fills the body's missing lanes and
 // must be a value the visitors ignore.
-template <class Visit, class Group>
+// NC: read-only loads (keys not written during the kernel); false: coherent loads, for a
+// kernel that moves the keys it reads (k_subtree).
+template <bool NC = true, class Visit, class Group>
 __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint32_t e1, float pad,
                                            uint32_t ti, uint32_t nt, Visit visit, Group group) {
+    auto ld = [](const float *p) { return NC ? __ldg(p) : *p; };
+    auto ld4 = [](const float4 *p) { return NC ? __ldg(p) : *p; };
     const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
     const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
-    for (uint32_t i = e0 + ti; i < a0; i += nt) visit(__ldg(keys + i));
+    for (uint32_t i = e0 + ti; i < a0; i += nt) visit(ld(keys + i));
     const uint32_t n4 = (e1 - a0) >> 2;
     const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
     for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * nt) {
@@ -626,7 +632,7 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
 #pragma unroll
         for (int u = 0; u < kHistVec; ++u) {
             const uint32_t j = j0 + u * nt + ti;
-            q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
+            q[u] = j < n4 ? ld4(k4 + j) : make_float4(pad, pad, pad, pad);
         }
         float k[kGroup];
 #pragma unroll
@@ -638,7 +644,7 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
         }
         group(k);
     }
-    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(__ldg(keys + i));
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(ld(keys + i));
 }
 
 // One count-left pass over the tiles of the level's active cells (cells of more than one
@@ -646,6 +652,7 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
 // added to the cell's global bins; sparse cells (few keys in the bracket, known from the
 // previous pass) send their bracket keys straight to the global bins.
 __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
     __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
@@ -778,6 +785,7 @@ constexpr int kListPerLane = 8;     // bracket keys a lane can hold
 constexpr uint32_t kListKeys = 64;  // bracket size that switches to the register list
 
 __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_bins[kThreads / 32][kTileBins];
     __shared__ float s_edges[kThreads / 32][kTileBins + 1];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -932,6 +940,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
 // Resolve: replay up to K bisection iterations per cell on its histogram (warp per cell).
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= v.C) return;
@@ -1047,6 +1056,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
 constexpr int kWarpKeysPerLane = kWarpKeys / 32;
 
 __global__ void __launch_bounds__(kThreads) k_bisect_warp(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= v.C || v.state[c] != kSmall) return;
@@ -1129,6 +1139,7 @@ constexpr size_t kCtaSmemBytes = kListCap * sizeof(float) +
                                  ((1u << kMaxBinsLog2) + 1) * sizeof(float);
 
 __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     extern __shared__ __align__(16) unsigned char cta_smem[];
     float *list = reinterpret_cast<float *>(cta_smem);
     uint32_t *s_hist = reinterpret_cast<uint32_t *>(list + kListCap);
@@ -1282,6 +1293,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
 // Tile -> cell maps of the level (one binary search per tile, once per level).
 // ... and the per-cell state of the level, in parallel (the plan only computes the offsets).
 __global__ void k_tile_map(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const uint32_t ht = v.tile_off[v.C], pt = v.ptile_off[v.C], C = (uint32_t)v.C;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < max(max(ht, pt), C);
          t += gridDim.x * blockDim.x) {
@@ -1335,6 +1347,7 @@ __device__ __forceinline__ unsigned long long pack_status(unsigned long long fla
 constexpr int kClassifyLoads = 16;
 
 __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_words[kThreads / 32][2][kPWords];
     const uint32_t total = v.ptile_off[v.C];
     const int lane = threadIdx.x & 31;
@@ -1400,6 +1413,7 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
 constexpr int kScanBlock = 1024;
 
 __global__ void __launch_bounds__(kScanBlock) k_tile_scan(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t sh[96];
     __shared__ uint32_t s_b;
     __shared__ uint32_t s_pre[2];
@@ -1512,6 +1526,7 @@ __device__ uint32_t warp_select(const uint32_t *bits, const uint32_t *pre, uint3
 //   s = max_x min(f(x), g(x)), f(x) = #{>= cut in [0,x)}, g(x) = #{<= cut in [x,n)}
 //   i = min(L_{s+1}, R_s); i == n marks the clamped case (every key below the cut).
 __global__ void __launch_bounds__(kThreads) k_part_cells(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= v.C) return;
@@ -1642,6 +1657,7 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #define ORB_SWAP_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t posL[kPTile];
     __shared__ uint32_t posR[kPTile];
     __shared__ uint32_t sh[96];
@@ -1734,15 +1750,12 @@ __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {
     c.cutMarginRight = c.upper[a];
 }
 
-// P5: final swap(i, n-1), children's ranges and (optionally) the children's cells.
-__global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= v.C) return;
-    const int slot = level_slot(v, c);
+// Final swap(i, n-1) of a partitioned cell (src/services/partition.cpp:52), its children's
+// ranges and (optionally) its children's cells.
+__device__ void finish_cell(const Level &v, int slot, uint32_t i, bool do_split) {
     const orb_cell_t cell = v.heap[slot];
     const uint2 rg = v.ranges[slot];
     const uint32_t n = rg.y - rg.x;
-    const uint32_t i = v.part_i[c];
     if (i < n) {
         if (i != n - 1) swap_particles(v, rg.x + i, rg.x + n - 1);
     } else {
@@ -1776,6 +1789,355 @@ __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split)
     set_axis_and_margin(lc, v.counters);
     v.heap[lslot] = lc;
     v.heap[rslot] = rc;
+}
+
+// P5: finish_cell for every cell of the level.
+__global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= v.C) return;
+    finish_cell(v, level_slot(v, c), v.part_i[c], do_split != 0);
+}
+
+// ------------------------------------------------------------------------------------
+// Subtrees: once every cell of a level holds at most kSubMax particles, one CTA takes a
+// cell and finishes all the levels below it (bisection, Hoare partition and split of each
+// descendant, breadth first), the same steps as the level kernels at CTA scale. A cell's
+// particles (at most 204 KB) stay in L2 across its levels instead of crossing DRAM once per
+// level, and the level kernels of those levels do not run.
+// ------------------------------------------------------------------------------------
+constexpr uint32_t kSubMax = kSubMaxParticles;  // particles of a cell a CTA can take (masks)
+constexpr int kSubWords = (int)(kSubMax / 32);
+constexpr int kSubThreads = 256;
+constexpr int kSubBinsLog2 = 9;
+constexpr int kSubQueue = 64;                 // descendants of one level held at once
+
+struct SubSmem {
+    uint32_t ge[kSubWords], le[kSubWords];           // key >= cut, key <= cut
+    uint32_t pge[kSubWords + 1], ple[kSubWords + 1];  // exclusive prefix popcounts
+    uint32_t bins[1 << kSubBinsLog2];
+    float edges[(1 << kSubBinsLog2) + 1];
+    uint32_t red[96];
+    int queue[2][kSubQueue];
+    uint32_t word;                                   // a broadcast value
+};
+
+// Position of the bit of rank r (0-based) in w (r < popc(w)).
+__device__ __forceinline__ uint32_t select_in_word(uint32_t w, uint32_t r) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const uint32_t c = (uint32_t)__popc(w & ((1u << step) - 1u));
+        if (r >= c) {
+            r -= c;
+            w >>= step;
+            pos += (uint32_t)step;
+        }
+    }
+    return pos;
+}
+
+// Position (cell-relative) of the set bit of rank r (0-based) of the mask `bits`, given
+// its exclusive word prefix `pre` over W words.
+__device__ __forceinline__ uint32_t sub_select(const uint32_t *bits, const uint32_t *pre, int W,
+                                               uint32_t r) {
+    int lo = 0, hi = W - 1;  // last word with pre <= r
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= r)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return (uint32_t)lo * 32u + select_in_word(bits[lo], r - pre[lo]);
+}
+
+// The reference's bisection (src/orbit.cpp:146-232) of one cell by the CTA: a warp with the
+// keys in registers for at most kWarpKeys keys, else rounds of a shared-memory histogram over
+// the midpoint tree of the bracket (tree depth from the keys left in it) each replaying up to
+// K iterations, as k_bisect_tile does per warp.
+__device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long long &bytes) {
+    orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    uint32_t it = 0;
+    int st = kActive;
+    if (n <= (uint32_t)kWarpKeys) {
+        if (tid < 32) {
+            float k[kWarpKeysPerLane];
+#pragma unroll
+            for (int j = 0; j < kWarpKeysPerLane; ++j) {
+                const uint32_t i = (uint32_t)(j * 32) + lane;
+                k[j] = i < n ? keys[rg.x + i] : __int_as_float(0x7fc00000);  // coherent: moved here
+            }
+            while (st == kActive) {
+                if (it >= (uint32_t)kMaxIterations) {
+                    st = kCapped;
+                    break;
+                }
+                const float cut = mid_cut(L, R);
+                uint32_t cnt = 0;
+#pragma unroll
+                for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
+                cnt = warp_sum(cnt);
+                ++it;
+                const int dir = convergence(cnt, n);
+                if (dir == 0)
+                    st = kFound;
+                else if (dir > 0)
+                    R = cut;
+                else
+                    L = cut;
+            }
+        }
+        if (tid == 0) bytes += 4ull * n;
+    } else {
+        uint32_t cand = n;
+        while (st == kActive) {
+            // about one key a bin once the bracket is small: two rounds for most cells
+            const int K = max(1, min(kSubBinsLog2, 32 - __clz(max(cand, 1u))));
+            const uint32_t nb = 1u << K;
+            for (uint32_t j = tid; j < nb; j += blockDim.x) sm.bins[j] = 0u;
+            fill_edges(sm.edges, L, R, K, tid, blockDim.x);
+            __syncthreads();
+            const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
+            const float m = bin_margin(L, R, scale, nb);
+            const float one_m = __fsub_rd(1.0f, m);
+            const int top = (int)nb - 1;
+            uint32_t below = 0;
+            auto one = [&](float k) {
+                if (k < L)
+                    ++below;
+                else if (k < R)
+                    atomicAdd(&sm.bins[fast_bin(k, L, scale, m, one_m, top, sm.edges)], 1u);
+            };
+            visit_keys<false>(keys, rg.x, rg.y, R, tid, blockDim.x, one, each(one));
+            if (tid == 0) bytes += 4ull * n;
+            below = block_sum(below, sm.red);
+            // exclusive prefix of the bins in place (each thread its own run)
+            const uint32_t per = max(1u, nb / blockDim.x), j0 = tid * per, j1 = min(nb, j0 + per);
+            uint32_t loc = 0;
+            for (uint32_t j = j0; j < j1; ++j) loc += sm.bins[j];
+            uint32_t tot, unused;
+            uint32_t run = block_excl_scan2(loc, 0u, sm.red, &tot, &unused).x;
+            for (uint32_t j = j0; j < j1; ++j) {
+                const uint32_t h = sm.bins[j];
+                sm.bins[j] = run;
+                run += h;
+            }
+            __syncthreads();
+            uint32_t pos = 0, width = nb;
+            for (int step = 0; step < K; ++step) {
+                if (it >= (uint32_t)kMaxIterations) {
+                    st = kCapped;
+                    break;
+                }
+                const uint32_t half = width >> 1;
+                const uint32_t cl = below + sm.bins[pos + half];
+                ++it;
+                const int dir = convergence(cl, n);
+                if (dir == 0) {
+                    st = kFound;
+                    break;
+                }
+                const float cut = mid_cut(L, R);
+                if (dir > 0) {
+                    R = cut;
+                } else {
+                    L = cut;
+                    pos += half;
+                }
+                width = half;
+            }
+            if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
+            if (st == kActive) cand = (pos + 1 < nb ? sm.bins[pos + 1] : tot) - sm.bins[pos];
+            __syncthreads();  // the bins are rewritten by the next round
+        }
+    }
+    if (tid == 0) {
+        cell.cutMarginLeft = L;
+        cell.cutMarginRight = R;
+        cell.foundCut = st == kFound ? 1 : 0;
+        atomicMax(&v.counters->max_iters, it);
+        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+    }
+    __syncthreads();
+}
+
+// Hoare partition of one cell by the CTA (same characterisation as the level kernels: the
+// pairs (L_k, R_k), k < s, swapped, then i = min(L_{s+1}, R_s) and swap(i, n-1)), then the
+// split into its children.
+__device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned long long &bytes) {
+    const orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x, b = rg.x;
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    const float cut = cell_cut(cell);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int W = (int)((n + 31) / 32);
+    // masks: a warp per word, kSubLoads words of a warp in flight at once
+    constexpr int kSubLoads = 8;
+    for (int w0 = (int)warp; w0 < W; w0 += (int)nwarps * kSubLoads) {
+        float k[kSubLoads];
+#pragma unroll
+        for (int u = 0; u < kSubLoads; ++u) {
+            const int w = w0 + u * (int)nwarps;
+            const uint32_t i = (uint32_t)w * 32u + lane;
+            k[u] = (w < W && i < n) ? keys[b + i] : 0.0f;  // coherent: the CTA moved these keys
+        }
+#pragma unroll
+        for (int u = 0; u < kSubLoads; ++u) {
+            const int w = w0 + u * (int)nwarps;
+            if (w >= W) break;
+            const bool valid = (uint32_t)w * 32u + lane < n;
+            const uint32_t gb = __ballot_sync(0xffffffffu, valid && !(k[u] < cut));
+            const uint32_t lb = __ballot_sync(0xffffffffu, valid && !(k[u] > cut));
+            if (lane == 0) {
+                sm.ge[w] = gb;
+                sm.le[w] = lb;
+            }
+        }
+    }
+    __syncthreads();
+    // exclusive prefix popcounts of both masks
+    const int per = (W + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int w0 = (int)tid * per, w1 = min(W, w0 + per);
+    uint32_t cg = 0, cl = 0;
+    for (int w = w0; w < w1; ++w) {
+        cg += __popc(sm.ge[w]);
+        cl += __popc(sm.le[w]);
+    }
+    uint32_t ge_tot, le_tot;
+    const uint2 ex = block_excl_scan2(cg, cl, sm.red, &ge_tot, &le_tot);
+    uint32_t rg_ = ex.x, rl = ex.y;
+    for (int w = w0; w < w1; ++w) {
+        sm.pge[w] = rg_;
+        sm.ple[w] = rl;
+        rg_ += __popc(sm.ge[w]);
+        rl += __popc(sm.le[w]);
+    }
+    if (tid == 0) {
+        sm.pge[W] = ge_tot;
+        sm.ple[W] = le_tot;
+    }
+    // s = max over x of min(#>= in [0,x), #<= in [x,n))
+    uint32_t best = 0;
+    {
+        uint32_t f = ex.x, g = le_tot - ex.y;
+        best = min(f, g);
+        for (int w = w0; w < w1; ++w) {
+            uint32_t a = sm.ge[w], c = sm.le[w];
+            for (int q = 0; q < 32; ++q) {
+                f += a & 1u;
+                g -= c & 1u;
+                a >>= 1;
+                c >>= 1;
+                best = max(best, min(f, g));
+            }
+        }
+    }
+    __syncthreads();  // prefixes complete
+    const uint32_t s_pairs = block_max(best, sm.red);
+    // split index i = min(L_{s+1}, R_s); n when every key is below the cut
+    if (tid == 0) {
+        uint32_t i = n;
+        if (ge_tot > s_pairs) i = min(i, sub_select(sm.ge, sm.pge, W, s_pairs));
+        if (s_pairs >= 1) i = min(i, sub_select(sm.le, sm.ple, W, le_tot - s_pairs));
+        sm.word = i;
+    }
+    // the swaps: pair k = (rank k of >=, rank le_tot-1-k of <=); sides disjoint; a thread
+    // loads kSubPairs pairs before it stores any
+    constexpr int kSubPairs = 2;
+    for (uint32_t k0 = tid; k0 < s_pairs; k0 += blockDim.x * kSubPairs) {
+        uint32_t pa[kSubPairs], pb[kSubPairs];
+        float xa[kSubPairs], xb[kSubPairs], ya[kSubPairs], yb[kSubPairs], za[kSubPairs], zb[kSubPairs];
+        uint32_t ia[kSubPairs], ib[kSubPairs];
+#pragma unroll
+        for (int q = 0; q < kSubPairs; ++q) {
+            const uint32_t k = k0 + q * blockDim.x;
+            pa[q] = pb[q] = 0xffffffffu;
+            if (k < s_pairs) {
+                pa[q] = b + sub_select(sm.ge, sm.pge, W, k);
+                pb[q] = b + sub_select(sm.le, sm.ple, W, le_tot - 1 - k);
+                xa[q] = v.x[pa[q]];
+                xb[q] = v.x[pb[q]];
+                ya[q] = v.y[pa[q]];
+                yb[q] = v.y[pb[q]];
+                za[q] = v.z[pa[q]];
+                zb[q] = v.z[pb[q]];
+                if (v.idx) {
+                    ia[q] = v.idx[pa[q]];
+                    ib[q] = v.idx[pb[q]];
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kSubPairs; ++q) {
+            if (pa[q] == 0xffffffffu) continue;
+            v.x[pa[q]] = xb[q];
+            v.x[pb[q]] = xa[q];
+            v.y[pa[q]] = yb[q];
+            v.y[pb[q]] = ya[q];
+            v.z[pa[q]] = zb[q];
+            v.z[pb[q]] = za[q];
+            if (v.idx) {
+                v.idx[pa[q]] = ib[q];
+                v.idx[pb[q]] = ia[q];
+            }
+        }
+    }
+    if (tid == 0) bytes += (v.idx ? 64ull : 48ull) * s_pairs + 4ull * n;
+    __syncthreads();  // swaps done, sm.word visible
+    if (tid == 0) finish_cell(v, slot, sm.word, true);
+    __syncthreads();
+}
+
+// Flag for k_subtree: every cell of the level fits a CTA and the tree below is at most
+// kSubLevels deep (the descendant queue). One CTA.
+constexpr int kSubLevels = kSubMaxLevels;
+static_assert((2 << (kSubLevels - 1)) <= kSubQueue, "the last level's children fit the queue");
+__global__ void __launch_bounds__(1024) k_subtree_check(Level v, int levels) {
+    __shared__ uint32_t sh[96];
+    uint32_t mx = 0;
+    for (int c = threadIdx.x; c < v.C; c += blockDim.x) {
+        const uint2 rg = v.ranges[level_slot(v, c)];
+        mx = max(mx, rg.y - rg.x);
+    }
+    mx = block_max(mx, sh);
+    if (threadIdx.x == 0) *v.skip = mx <= kSubMax && levels <= kSubLevels ? 1u : 0u;
+}
+
+// One CTA per cell of the level: all `levels` levels below it, breadth first.
+__global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v, int levels) {
+    __shared__ SubSmem sm;
+    if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
+    unsigned long long bytes = 0;
+    for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
+        int cur = 0, nq = 1;
+        if (threadIdx.x == 0) sm.queue[0][0] = level_slot(v, c);
+        __syncthreads();
+        for (int l = 0; l < levels; ++l) {
+            int nn = 0;
+            for (int q = 0; q < nq; ++q) {
+                const int slot = sm.queue[cur][q];
+                sub_bisect(v, slot, sm, bytes);
+                sub_partition(v, slot, sm, bytes);
+                if (threadIdx.x == 0 && nn + 2 <= kSubQueue) {
+                    const int id = v.heap[slot].id;
+                    sm.queue[cur ^ 1][nn] = slot + id + 1;
+                    sm.queue[cur ^ 1][nn + 1] = slot + id + 2;
+                }
+                nn += 2;
+            }
+            __syncthreads();
+            cur ^= 1;
+            nq = nn;
+        }
+    }
+    if (threadIdx.x == 0 && bytes) add_bytes(v, kKSubtree, bytes);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1953,6 +2315,8 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
+        case kKSubtreeCheck: k_subtree_check<<<1, 1024, 0, st>>>(v, arg); break;
+        case kKSubtree: k_subtree<<<grid, kSubThreads, 0, st>>>(v, arg); break;
         case kKBisectCta:
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;

@@ -199,3 +199,17 @@ def test_headline_properties(ctx, oracle, engine):
     leaves = res.ranges[(1 << 16) - 1:]
     sizes = leaves[:, 1].astype(np.int64) - leaves[:, 0]
     assert sizes.min() >= 2048 - 64 and sizes.max() <= 2048 + 64
+
+
+@pytest.mark.parametrize("kind,seed,logn,logd", [("plummer", 501, 20, 15), ("uniform", 502, 21, 12),
+                                                 ("plummer", 503, 19, 13)])
+def test_subtree_levels_match_oracle(ctx, oracle, kind, seed, logn, logd):
+    # deep trees whose last levels (cells of at most ~17K particles, up to 6 levels) are
+    # finished by one CTA per cell
+    gen = oracle.gen_uniform if kind == "uniform" else oracle.gen_plummer
+    x, y, z = gen(seed, 1 << logn)
+    ref = oracle.build_tree(x, y, z, 1 << logd)
+    r = ctx.build(x.copy(), y.copy(), z.copy(), 1 << logd)
+    assert r.heap.tobytes() == ref.heap.tobytes()
+    assert np.array_equal(r.ranges, ref.ranges[0])
+    assert np.array_equal(r.perm, ref.perm)
