@@ -405,7 +405,7 @@ def gpu_arm(args):
     t0 = time.perf_counter()
     if args.tuning:
         names = ("hist_blocks_per_sm", "part_blocks_per_sm", "tile_blocks_per_sm",
-                 "sparse_keys_per_tile", "cta_min_cells")
+                 "sparse_keys_per_tile", "cta_min_cells", "subtree_levels")
         ctx.set_tuning(**dict(zip(names, (int(v) for v in args.tuning.split(",")))))
         tuning, tuned_by = ctx.get_tuning(), "--tuning"
     else:
@@ -599,7 +599,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--tuning", default=None,
-                    help="hist,part,tile,sparse,cta: use this launch tuning for the headline "
+                    help="hist,part,tile,sparse,cta,subtree: use this launch tuning for the headline "
                          "instead of autotuning it (profiling runs reuse a chosen setting)")
     args = ap.parse_args()
     if args.impl == "reference":

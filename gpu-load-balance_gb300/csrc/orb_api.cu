@@ -73,7 +73,7 @@ struct orb_ctx {
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint32_t> htile_cell, ptile_cell;
     // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
-    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u};
+    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 3u};
     DevBuf<uint8_t> hist_k, state, iters, listed, cmp_bad;
     DevBuf<uint32_t> cmp_off, cmp_cnt;
     DevBuf<float> cmp_keys;
@@ -396,7 +396,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
     for (uint32_t t : {ctx->tune.hist_blocks_per_sm, ctx->tune.part_blocks_per_sm, ctx->tune.tile_blocks_per_sm,
-                       ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells})
+                       ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells, ctx->tune.subtree_levels})
         key.push_back(t);
     return key;
 }
@@ -437,6 +437,22 @@ struct LevelDesc {
 // The reference's level loop (src/orbit.cpp:102-275) over every cell of every level: plan,
 // bisection (one warp for small cells, one CTA per cell or the multi-CTA histogram passes
 // for the rest), partition and split.
+// The level from which subtree CTAs finish the tree (-1: none): the first level whose cells
+// (at most max_n >> l particles plus a few per split: each split leaves a cell within 3 of
+// half) all fit one CTA, that has enough cells to fill the GPU, and that is at most
+// tune.subtree_levels levels above the leaves. full: every tree is built to its leaves.
+int subtree_from(const orb_ctx *ctx, const std::vector<LevelDesc> &lv, uint64_t max_n, bool full) {
+    const uint32_t want = std::min<uint32_t>(ctx->tune.subtree_levels, (uint32_t)kSubMaxLevels);
+    if (!full || want == 0) return -1;
+    for (size_t li = 0; li < lv.size(); ++li) {
+        const uint64_t expect = (max_n >> li) + 1 + 8ull * li;
+        if (expect <= kSubMaxParticles && (uint64_t)lv[li].C >= 2ull * (uint64_t)ctx->num_sms &&
+            lv.size() - li <= want)
+            return (int)li;
+    }
+    return -1;
+}
+
 // sub_from >= 0: from level lv[sub_from] down, one CTA per cell finishes the tree when every
 // cell of that level fits one (k_subtree_check decides on the device); the level kernels of
 // those levels then return at once.
@@ -451,8 +467,7 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         if ((int)li == sub_from) {
             v.skip = ctx->sub_flag.p;
             run_kernel(ctx, kKSubtreeCheck, v, 1, (int)(lv.size() - li));
-            run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm),
-                       (int)(lv.size() - li));
+            run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm));
         }
         run_kernel(ctx, kKPlan, v, 1);
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
@@ -653,18 +668,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         key_add_f(key, lower[a]);
         key_add_f(key, upper[a]);
     }
-    // subtrees from the first level whose cells (about n / 2^l, each split moving a cell's
-    // count by at most a few particles from half) all fit one CTA, once there are enough
-    // cells to fill the GPU
-    int sub_from = -1;
-    for (size_t li = 0; li < lv.size(); ++li) {
-        const uint64_t expect = (n >> li) + 1 + 8ull * li;
-        if (expect <= kSubMaxParticles && (uint64_t)lv[li].C >= 2ull * ctx->num_sms &&
-            lv.size() - li <= (size_t)kSubMaxLevels) {
-            sub_from = (int)li;
-            break;
-        }
-    }
+    const int sub_from = subtree_from(ctx, lv, n, levels == (uint32_t)ylev);
     if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
     key.push_back((uint64_t)(int64_t)sub_from);
     uint32_t passes = 0;
@@ -1125,6 +1129,16 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
             key_add_f(key, inst[i].upper[a]);
         }
     }
+    // subtrees when every instance is built to its leaves (warm builds keep the level path)
+    bool full = !warm;
+    uint64_t max_n = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        full = full && lev[i] == (uint32_t)log2_exact(inst[i].d);
+        max_n = std::max<uint64_t>(max_n, inst[i].n);
+    }
+    const int sub_from = subtree_from(ctx, lv, max_n, full);
+    if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
+    key.push_back((uint64_t)(int64_t)sub_from);
     uint32_t passes = 0;
     st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
         ORB_CUDA(cudaMemsetAsync(ctx->heap.p, 0, heap_cells * sizeof(orb_cell_t), s));
@@ -1133,7 +1147,7 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
         ctx->launches[kKInit] += 1;
         launch_init_batch(v, ctx->batch_roots.p, (int)k, n_total, s);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp);
+        return run_levels(ctx, v, lv, pp, sub_from);
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
@@ -1247,7 +1261,7 @@ static bool tuning_valid(const orb_tuning &t) {
     return t.hist_blocks_per_sm >= 1 && t.hist_blocks_per_sm <= 8 &&
            t.part_blocks_per_sm >= 1 && t.part_blocks_per_sm <= 16 && t.tile_blocks_per_sm >= 1 &&
            t.tile_blocks_per_sm <= 8 && t.sparse_keys_per_tile >= 1 &&
-           t.sparse_keys_per_tile <= (uint32_t)kTile;
+           t.sparse_keys_per_tile <= (uint32_t)kTile && t.subtree_levels <= (uint32_t)kSubMaxLevels;
 }
 
 orb_status orb_set_tuning(orb_ctx *ctx, const orb_tuning *t) {
@@ -1328,7 +1342,8 @@ orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, cons
     }
     // coordinate descent over result-invariant parameters
     static const uint32_t hist_c[] = {4, 6, 8}, part_c[] = {4, 8, 16}, tile_c[] = {2, 4},
-                          sparse_c[] = {16, 64, 256}, cta_c[] = {0, 512, 4096};
+                          sparse_c[] = {16, 64, 256}, cta_c[] = {0, 512, 4096},
+                          sub_c[] = {0, 2, 3, 4, 6};
     struct Axis {
         uint32_t orb_tuning::*field;
         const uint32_t *vals;
@@ -1338,7 +1353,8 @@ orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, cons
                          {&orb_tuning::part_blocks_per_sm, part_c, 3},
                          {&orb_tuning::tile_blocks_per_sm, tile_c, 2},
                          {&orb_tuning::sparse_keys_per_tile, sparse_c, 3},
-                         {&orb_tuning::cta_min_cells, cta_c, 3}};
+                         {&orb_tuning::cta_min_cells, cta_c, 3},
+                         {&orb_tuning::subtree_levels, sub_c, 5}};
     for (const Axis &ax : axes) {
         const orb_tuning base = cur;
         for (int i = 0; i < ax.n; ++i) {

@@ -2095,29 +2095,41 @@ __device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned lo
     __syncthreads();
 }
 
-// Flag for k_subtree: every cell of the level fits a CTA and the tree below is at most
-// kSubLevels deep (the descendant queue). One CTA.
-constexpr int kSubLevels = kSubMaxLevels;
-static_assert((2 << (kSubLevels - 1)) <= kSubQueue, "the last level's children fit the queue");
-__global__ void __launch_bounds__(1024) k_subtree_check(Level v, int levels) {
-    __shared__ uint32_t sh[96];
-    uint32_t mx = 0;
-    for (int c = threadIdx.x; c < v.C; c += blockDim.x) {
-        const uint2 rg = v.ranges[level_slot(v, c)];
-        mx = max(mx, rg.y - rg.x);
-    }
-    mx = block_max(mx, sh);
-    if (threadIdx.x == 0) *v.skip = mx <= kSubMax && levels <= kSubLevels ? 1u : 0u;
+// Levels below a cell in a full build: log2 of its leaf count (d is a power of two).
+__device__ __forceinline__ int levels_below(const orb_cell_t &c) {
+    return c.nLeafCells > 1 ? 31 - __clz((uint32_t)c.nLeafCells) : 0;
 }
 
-// One CTA per cell of the level: all `levels` levels below it, breadth first.
-__global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v, int levels) {
+// Flag for k_subtree: every cell of the level fits a CTA and has at most `max_levels`
+// (<= kSubLevels, the descendant queue) levels below it. One CTA.
+constexpr int kSubLevels = kSubMaxLevels;
+static_assert((2 << (kSubLevels - 1)) <= kSubQueue, "the last level's children fit the queue");
+__global__ void __launch_bounds__(1024) k_subtree_check(Level v, int max_levels) {
+    __shared__ uint32_t sh[96];
+    uint32_t mx = 0, ml = 0;
+    for (int c = threadIdx.x; c < v.C; c += blockDim.x) {
+        const int slot = level_slot(v, c);
+        const uint2 rg = v.ranges[slot];
+        mx = max(mx, rg.y - rg.x);
+        ml = max(ml, (uint32_t)levels_below(v.heap[slot]));
+    }
+    mx = block_max(mx, sh);
+    ml = block_max(ml, sh);
+    if (threadIdx.x == 0)
+        *v.skip = mx <= kSubMax && (int)ml <= min(max_levels, kSubLevels) ? 1u : 0u;
+}
+
+// One CTA per cell of the level: every level below it (its leaf count's log2), breadth
+// first.
+__global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
     unsigned long long bytes = 0;
     for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
         int cur = 0, nq = 1;
-        if (threadIdx.x == 0) sm.queue[0][0] = level_slot(v, c);
+        const int root = level_slot(v, c);
+        const int levels = levels_below(v.heap[root]);
+        if (threadIdx.x == 0) sm.queue[0][0] = root;
         __syncthreads();
         for (int l = 0; l < levels; ++l) {
             int nn = 0;
@@ -2316,7 +2328,7 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
         case kKSubtreeCheck: k_subtree_check<<<1, 1024, 0, st>>>(v, arg); break;
-        case kKSubtree: k_subtree<<<grid, kSubThreads, 0, st>>>(v, arg); break;
+        case kKSubtree: k_subtree<<<grid, kSubThreads, 0, st>>>(v); break;
         case kKBisectCta:
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;

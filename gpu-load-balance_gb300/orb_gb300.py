@@ -130,6 +130,7 @@ class Tuning(ctypes.Structure):
         ("tile_blocks_per_sm", ctypes.c_uint32),
         ("sparse_keys_per_tile", ctypes.c_uint32),
         ("cta_min_cells", ctypes.c_uint32),
+        ("subtree_levels", ctypes.c_uint32),
     ]
 
     def as_dict(self):

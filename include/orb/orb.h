@@ -185,6 +185,9 @@ typedef struct orb_tuning {
                                       this many keys per tile, 1..16384 (default 64) */
     uint32_t cta_min_cells;        /* levels with at least this many cells bisect one cell per
                                       CTA; 0 = never (default) */
+    uint32_t subtree_levels;       /* the last levels (at most this many, 0..6, default 3) are
+                                      finished by one CTA per cell once every cell of a level
+                                      fits one (at most 17408 particles); 0 = never */
 } orb_tuning;
 
 orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out);

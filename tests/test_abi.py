@@ -50,8 +50,8 @@ def test_cell_layout(engine):
 
 
 def test_tuning_layout_and_null_checks(engine):
-    # orb_tuning: five uint32 fields, no padding
-    assert ctypes.sizeof(engine.Tuning) == 20
+    # orb_tuning: six uint32 fields, no padding
+    assert ctypes.sizeof(engine.Tuning) == 24
     lib = engine.load()
     t = engine.Tuning()
     assert lib.orb_get_tuning(None, ctypes.byref(t)) == 1
