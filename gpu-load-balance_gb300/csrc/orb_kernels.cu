@@ -1812,14 +1812,19 @@ constexpr int kSubThreads = 256;
 constexpr int kSubBinsLog2 = 9;
 constexpr int kSubQueue = 64;                 // descendants of one level held at once
 
+constexpr int kSubList = 256;                 // bracket keys gathered for the last iterations
+constexpr int kSubRankBlocks = (int)(kSubMax / 64) + 2;
+
 struct SubSmem {
     uint32_t ge[kSubWords], le[kSubWords];           // key >= cut, key <= cut
     uint32_t pge[kSubWords + 1], ple[kSubWords + 1];  // exclusive prefix popcounts
+    uint16_t tge[kSubRankBlocks], tle[kSubRankBlocks];  // word holding rank 64 b
     uint32_t bins[1 << kSubBinsLog2];
     float edges[(1 << kSubBinsLog2) + 1];
+    float list[kSubList];
     uint32_t red[96];
     int queue[2][kSubQueue];
-    uint32_t word;                                   // a broadcast value
+    uint32_t word, count;                            // broadcast values
 };
 
 // Position of the bit of rank r (0-based) in w (r < popc(w)).
@@ -1835,6 +1840,15 @@ __device__ __forceinline__ uint32_t select_in_word(uint32_t w, uint32_t r) {
         }
     }
     return pos;
+}
+
+// sub_select() through the rank table t (t[b] = the word holding rank 64 b): a few steps
+// from the table's word instead of a search.
+__device__ __forceinline__ uint32_t sub_select_t(const uint32_t *bits, const uint32_t *pre,
+                                                 const uint16_t *t, uint32_t r) {
+    uint32_t w = t[r >> 6];
+    while (pre[w + 1] <= r) ++w;
+    return w * 32u + select_in_word(bits[w], r - pre[w]);
 }
 
 // Position (cell-relative) of the set bit of rank r (0-based) of the mask `bits`, given
@@ -1954,7 +1968,49 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
             }
             if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
             if (st == kActive) cand = (pos + 1 < nb ? sm.bins[pos + 1] : tot) - sm.bins[pos];
+            const uint32_t below_L = below + sm.bins[pos];  // keys below the new L
             __syncthreads();  // the bins are rewritten by the next round
+            if (st == kActive && cand <= (uint32_t)kSubList) {
+                // the bracket's keys into a shared list; warp 0 finishes the bisection on it
+                if (tid == 0) sm.count = 0;
+                __syncthreads();
+                auto gather = [&](float k) {
+                    if (!(k < L) && k < R) sm.list[atomicAdd(&sm.count, 1u)] = k;
+                };
+                visit_keys<false>(keys, rg.x, rg.y, R, tid, blockDim.x, gather, each(gather));
+                if (tid == 0) bytes += 4ull * n;
+                __syncthreads();
+                if (tid < 32) {
+                    const uint32_t m = sm.count;
+                    constexpr int kPer = kSubList / 32;
+                    float kl[kPer];
+#pragma unroll
+                    for (int q = 0; q < kPer; ++q) {
+                        const uint32_t i = (uint32_t)q * 32u + lane;
+                        kl[q] = i < m ? sm.list[i] : R;  // R: never below a cut in [L, R]
+                    }
+                    while (st == kActive) {
+                        if (it >= (uint32_t)kMaxIterations) {
+                            st = kCapped;
+                            break;
+                        }
+                        const float cut = mid_cut(L, R);
+                        uint32_t c = 0;
+#pragma unroll
+                        for (int q = 0; q < kPer; ++q) c += kl[q] < cut;
+                        const uint32_t cl = below_L + warp_sum(c);
+                        ++it;
+                        const int dir = convergence(cl, n);
+                        if (dir == 0)
+                            st = kFound;
+                        else if (dir > 0)
+                            R = cut;
+                        else
+                            L = cut;
+                    }
+                }
+                break;  // warp 0 holds the result (thread 0 writes it)
+            }
         }
     }
     if (tid == 0) {
@@ -2023,24 +2079,40 @@ __device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned lo
         sm.pge[W] = ge_tot;
         sm.ple[W] = le_tot;
     }
-    // s = max over x of min(#>= in [0,x), #<= in [x,n))
-    uint32_t best = 0;
-    {
-        uint32_t f = ex.x, g = le_tot - ex.y;
-        best = min(f, g);
-        for (int w = w0; w < w1; ++w) {
-            uint32_t a = sm.ge[w], c = sm.le[w];
+    __syncthreads();  // prefixes complete
+    // rank tables: the word holding rank 64 b of each mask
+    for (int w = (int)tid; w < W; w += (int)blockDim.x) {
+        for (uint32_t r = (sm.pge[w] + 63u) & ~63u; r < sm.pge[w + 1]; r += 64u) sm.tge[r >> 6] = (uint16_t)w;
+        for (uint32_t r = (sm.ple[w] + 63u) & ~63u; r < sm.ple[w + 1]; r += 64u) sm.tle[r >> 6] = (uint16_t)w;
+    }
+    // s = max over x of min(#>= in [0,x), #<= in [x,n)): min(f, g) rises while f < g and
+    // falls after, so the maximum lies in the first word at whose end f >= g (one thread)
+    if (tid == 0) {
+        uint32_t s_max = 0;
+        if (W > 0) {
+            int lo = 0, hi = W - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (sm.pge[mid + 1] >= le_tot - sm.ple[mid + 1])
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            uint32_t f = sm.pge[lo], g = le_tot - sm.ple[lo];
+            uint32_t a = sm.ge[lo], c = sm.le[lo];
+            s_max = min(f, g);
             for (int q = 0; q < 32; ++q) {
                 f += a & 1u;
                 g -= c & 1u;
                 a >>= 1;
                 c >>= 1;
-                best = max(best, min(f, g));
+                s_max = max(s_max, min(f, g));
             }
         }
+        sm.count = s_max;
     }
-    __syncthreads();  // prefixes complete
-    const uint32_t s_pairs = block_max(best, sm.red);
+    __syncthreads();
+    const uint32_t s_pairs = sm.count;
     // split index i = min(L_{s+1}, R_s); n when every key is below the cut
     if (tid == 0) {
         uint32_t i = n;
@@ -2060,8 +2132,8 @@ __device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned lo
             const uint32_t k = k0 + q * blockDim.x;
             pa[q] = pb[q] = 0xffffffffu;
             if (k < s_pairs) {
-                pa[q] = b + sub_select(sm.ge, sm.pge, W, k);
-                pb[q] = b + sub_select(sm.le, sm.ple, W, le_tot - 1 - k);
+                pa[q] = b + sub_select_t(sm.ge, sm.pge, sm.tge, k);
+                pb[q] = b + sub_select_t(sm.le, sm.ple, sm.tle, le_tot - 1 - k);
                 xa[q] = v.x[pa[q]];
                 xb[q] = v.x[pb[q]];
                 ya[q] = v.y[pa[q]];
