@@ -128,8 +128,8 @@ def traffic_ratio(kernel: str):
     smaller case of the same workload; the ratio is per swapped pair / per key, so it scales
     with the units a launch processes)."""
     names = {"part_swap": "k_part_swap", "count_left_hist": "k_hist", "part_classify": "k_part_classify",
-             "bisect_tile": "k_bisect_tile"}
-    path = os.path.join(ROOT, "profiles", "dram_traffic_part_swap_hist_classify_2p24_2p12.txt")
+             "bisect_tile": "k_bisect_tile", "subtree": "k_subtree"}
+    path = os.path.join(ROOT, "profiles", "dram_traffic_part_swap_hist_classify_subtree_2p24_2p13.txt")
     try:
         with open(path) as f:
             for line in f:
@@ -523,7 +523,7 @@ def gpu_arm(args):
         "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
         "traffic": (ratio * dk["bytes"] / dk["launches"]) if ratio else None,
-        "traffic_source": "ncu dram bytes per algorithmic byte, 2^24/2^12 capture scaled per unit"
+        "traffic_source": "ncu dram bytes per algorithmic byte, 2^24/2^13 capture scaled per unit"
                           if ratio else None,
         "dram_gbs_equivalent": round(achieved * ratio, 1) if ratio else None,
         "bytes_per_launch": dk["bytes"] / dk["launches"],

@@ -487,15 +487,45 @@ __device__ __noinline__ int edge_bin_slow(float k, float L, float scale, int top
     return edge_bin(k, L, scale, top, [&](int j) { return e[j]; });
 }
 
-// edge_bin() with the scaled guess accepted outright when it is clear of both edges by the
-// margin m (bin_margin); L <= k < R.
-__device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, float one_m,
-                                        int top, const float *e) {
-    const float t = __fmul_rn(__fsub_rn(k, L), scale);
-    const int g = __float2int_rz(t);
-    const float f = __fsub_rn(t, __int2float_rn(g));
-    if (g <= top && f > m && f < one_m) return g;
-    return edge_bin_slow(k, L, scale, top, e);
+// The scaled guess with no float<->int conversion. For a key whose guess t = (k-L) scale lies
+// in [0, 2^11), y = fl(fl(k-L) scale + 2^11) is 2^11 + t rounded to 12 fraction bits, so the
+// encoding of y minus that of 2^11 holds the bin above bit 12 and the fraction below it. Its
+// error is that of fl(fl(k-L) scale) except the last rounding, 2^-13 bins instead of
+// t 2^-24, which the margin taken at 2^11 bins or more (2^-10) covers. The guess is exact
+// when its fraction f = i/4096 lies in (m, 1 - m), i.e. i in [mi+1, 4095-mi] with
+// mi = floor(4096 m) (4096 m is exact). `base` is the encoding of 2^11 plus mi+1, so the test
+// is a subtraction and two unsigned comparisons; a key below L (y under 2^11 or negative),
+// at or past R (a bin past the table) or NaN fails it.
+static_assert(kMaxBinsLog2 <= 11, "guess_bin holds bins below 2^11");
+struct Guess {
+    float L, scale;
+    uint32_t base, lim, span;
+};
+
+__device__ __forceinline__ Guess make_guess(float L, float R, float scale, uint32_t nb) {
+    Guess g;
+    g.L = L;
+    g.scale = scale;
+    const float M = __fmul_rn(bin_margin(L, R, scale, max(nb, 2048u)), 4096.0f);
+    const uint32_t mi = M < 2048.0f ? (uint32_t)M : 0u;  // M >= 2048 or NaN: accept nothing
+    g.base = __float_as_uint(2048.0f) + mi + 1u;
+    g.lim = nb << 12;
+    g.span = M < 2048.0f ? 4095u - 2u * mi : 0u;
+    return g;
+}
+
+// The guessed bin of k in *b; true when it is the exact bin (edge_bin's answer).
+__device__ __forceinline__ bool guess_bin(const Guess &g, float k, uint32_t *b) {
+    const uint32_t e = __float_as_uint(__fmaf_rn(__fsub_rn(k, g.L), g.scale, 2048.0f)) - g.base;
+    *b = e >> 12;
+    return e < g.lim && (e & 0xfffu) < g.span;
+}
+
+// edge_bin() with the guess accepted outright when guess_bin() proves it; L <= k < R.
+__device__ __forceinline__ int fast_bin(float k, const Guess &g, int top, const float *e) {
+    uint32_t b;
+    if (guess_bin(g, k, &b)) return (int)b;
+    return edge_bin_slow(k, g.L, g.scale, top, e);
 }
 
 
@@ -503,17 +533,36 @@ __device__ __forceinline__ int fast_bin(float k, float L, float scale, float m, 
 // One bracket key of a sparse pass into the cell's bins (global, or shared for a sparse
 // pass whose bracket holds more than kSparseGlobalKeys keys a tile), out of line as above.
 constexpr uint32_t kSparseGlobalKeys = 8;
-constexpr int kCmpTile = 1024;  // bracket keys a tile can compact (more: the cell keeps no list)
+constexpr int kCmpTile = 1024;  // bracket keys a CTA compacts for one cell's run of tiles (more:
+                                // the cell keeps no list)
+
+// The cell a count pass's CTA is working on, in shared memory (thread 0 fills it when the
+// CTA's tiles move to a new cell): the out-of-line paths read it there, so the streaming loop
+// keeps only what it needs in registers.
+constexpr uint32_t kHDense = 1, kHLocal = 2, kHCompact = 4, kHListed = 8;
+struct HistCell {
+    const float *keys;  // the cut axis
+    uint32_t *gh;       // the cell's global bins
+    float L, R, scale;
+    int K;
+    uint32_t mode;      // kHDense, else sparse (kHLocal: bracket keys to shared bins first;
+                        // kHCompact: and to the list), or kHListed
+    uint32_t base, end; // the cell's key range [base, end)
+    uint32_t t0;        // its first tile
+    uint32_t below;     // dense: keys below L met by the exact path
+    Guess gs;           // dense: the scaled guess
+};
 
 // Count pass over a cell whose bracket keys an earlier pass compacted: tile j of the cell
 // takes list keys [j kTile, (j+1) kTile) and bins those inside [L, R) (the keys below L are
-// already counted: resolve carried them). Returns the keys read. Out of line: the streaming
-// loop's registers stay its own.
-__device__ __noinline__ uint32_t listed_tile(const Level &v, const TileRef &tr, float L, float R,
-                                             int K, uint32_t *gh) {
-    const uint32_t cnt = v.cmp_cnt[tr.c];
-    const uint32_t lo = tr.local * (uint32_t)kTile, hi = min(cnt, lo + (uint32_t)kTile);
-    const float *list = v.cmp_keys + v.cmp_off[tr.c];
+// already counted: resolve carried them). Returns the keys read.
+__device__ __noinline__ uint32_t listed_tile(const Level &v, int c, uint32_t local, const HistCell *hc) {
+    const float L = hc->L, R = hc->R;
+    const int K = hc->K;
+    uint32_t *gh = hc->gh;
+    const uint32_t cnt = v.cmp_cnt[c];
+    const uint32_t lo = local * (uint32_t)kTile, hi = min(cnt, lo + (uint32_t)kTile);
+    const float *list = v.cmp_keys + v.cmp_off[c];
     for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const float k = list[i];
         if (k >= L && k < R) atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
@@ -521,11 +570,14 @@ __device__ __noinline__ uint32_t listed_tile(const Level &v, const TileRef &tr, 
     return hi > lo ? hi - lo : 0u;
 }
 
-// Appends a sparse tile's compacted bracket keys (nk of them in s_cmp) to its cell's list:
-// one reservation per tile; an overflow (of the tile's buffer or the list) marks the cell
-// as having no list. Returns the keys written. Every thread of the CTA calls it.
-__device__ __noinline__ uint32_t append_list(const Level &v, int c, const float *s_cmp, uint32_t nk,
+// Appends the bracket keys a CTA compacted for cell c (*s_ncmp of them in s_cmp) to the cell's
+// list and clears the count: one reservation per run of the cell's tiles; an overflow (of the
+// buffer or the list) marks the cell as having no list. Returns the keys written. Every
+// thread of the CTA calls it once its scans are done.
+__device__ __noinline__ uint32_t append_list(const Level &v, int c, const float *s_cmp, uint32_t *s_ncmp,
                                              uint32_t *s_base) {
+    __syncthreads();  // every key of the tile kept
+    const uint32_t nk = *s_ncmp;
     if (threadIdx.x == 0) {
         const uint32_t cap = v.cmp_off[c + 1] - v.cmp_off[c];
         *s_base = 0xffffffffu;
@@ -541,6 +593,7 @@ __device__ __noinline__ uint32_t append_list(const Level &v, int c, const float 
     }
     __syncthreads();
     const uint32_t b = *s_base;
+    if (threadIdx.x == 0) *s_ncmp = 0;
     uint32_t wrote = 0;
     if (b != 0xffffffffu) {
         float *list = v.cmp_keys + v.cmp_off[c] + b;
@@ -550,9 +603,35 @@ __device__ __noinline__ uint32_t append_list(const Level &v, int c, const float 
     __syncthreads();  // s_cmp and the count are reused by the next tile
     return wrote;
 }
-__device__ __noinline__ void add_sparse(uint32_t *gh, float k, float L, float R, int K) {
-    atomicAdd(&gh[tree_bin(k, L, R, K)], 1u);
+
+// A sparse pass's bracket key (L <= k < R): into the cell's bins (shared when kHLocal) and,
+// with kHCompact, into the tile's list buffer.
+__device__ __noinline__ void sparse_key(float k, const HistCell *hc, uint32_t *s_hist, float *s_cmp,
+                                        uint32_t *s_ncmp) {
+    const uint32_t mode = hc->mode;
+    const uint32_t b = (uint32_t)tree_bin(k, hc->L, hc->R, hc->K);
+    atomicAdd(mode & kHLocal ? &s_hist[b] : &hc->gh[b], 1u);
+    if (mode & kHCompact) {
+        const uint32_t i = atomicAdd(s_ncmp, 1u);
+        if (i < (uint32_t)kCmpTile) s_cmp[i] = k;
+    }
 }
+
+// A dense pass's key the scaled guess did not settle: below L counted, inside [L, R) binned
+// by the reference's descent (tree_bin), at or past R (or NaN) ignored.
+__device__ __noinline__ void dense_exact(float k, HistCell *hc, uint32_t *s_hist) {
+    const float L = hc->L, R = hc->R;
+    if (k < L)
+        atomicAdd(&hc->below, 1u);
+    else if (k < R)
+        atomicAdd(&s_hist[tree_bin(k, L, R, hc->K)], 1u);
+}
+
+// A compile-time flag passed to a generic lambda.
+template <bool B>
+struct Flag {
+    static constexpr bool value = B;
+};
 
 // Keys per thread per round of the histogram pass (float4 loads issued together).
 constexpr int kHistVec = 4;
@@ -566,23 +645,27 @@ constexpr int kGroup = 4 * kHistVec;  // keys a thread holds per round
 // through visit(k). `pad` fills the body's missing lanes: settle(pad) must count nothing
 // (a pad it leaves is skipped by the walk).
 static_assert(kTile / (4 * kHistVec * kThreads) <= 4, "scan_tile keeps 16 bits a round, 4 rounds");
-template <class Settle, class Rest, class Visit>
+template <uint32_t NT, class Settle, class Rest, class Visit>
 __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32_t e1, float pad,
                                           Settle settle, Rest rest, Visit visit) {
-    const uint32_t ti = threadIdx.x, nt = blockDim.x;
+    const uint32_t ti = threadIdx.x, nt = NT;  // NT = blockDim.x
     const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
     const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
     for (uint32_t i = e0 + ti; i < a0; i += nt) visit(__ldg(keys + i));
     const uint32_t n4 = (e1 - a0) >> 2;
     const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
     unsigned long long left = 0;  // bit 16 r + 4 u + c: component c of load u of round r
-    uint32_t r = 0;
-    for (uint32_t j0 = 0; j0 < n4; j0 += kHistVec * nt, ++r) {
+    uint32_t r = 0, j0 = 0;
+    // one round: kHistVec float4 loads in flight, then the 16 keys; Full: every load in range
+    auto round = [&](auto full) {
         float4 q[kHistVec];
 #pragma unroll
         for (int u = 0; u < kHistVec; ++u) {
             const uint32_t j = j0 + u * nt + ti;
-            q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
+            if (decltype(full)::value)
+                q[u] = __ldg(k4 + j);
+            else
+                q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
         }
         uint32_t miss = 0;
 #pragma unroll
@@ -592,7 +675,9 @@ __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32
             for (int c = 0; c < 4; ++c) miss |= (uint32_t)!settle(kk[c]) << (4 * u + c);
         }
         left |= (unsigned long long)miss << (16u * r);
-    }
+    };
+    for (; j0 + kHistVec * nt <= n4; j0 += kHistVec * nt, ++r) round(Flag<true>());
+    if (j0 < n4) round(Flag<false>());
     while (left) {
         const int b = __ffsll((long long)left) - 1;
         left &= left - 1;
@@ -647,127 +732,158 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
     for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(ld(keys + i));
 }
 
+// Whether pass v.pass over cell c (`tiles` tiles) is sparse: only the bracket's keys are
+// binned, the keys below it counted. The first pass of a cold level is dense for every cell;
+// later passes are sparse once the bracket holds at most sparse_per_tile keys a tile.
+__device__ __forceinline__ bool sparse_pass(const Level &v, int c, uint32_t tiles) {
+    return !(v.pass == 0 && v.warm == nullptr) && v.inb[c] <= v.sparse_per_tile * tiles;
+}
+
 // One count-left pass over the tiles of the level's active cells (cells of more than one
-// tile; a tile loop over all CTAs). Dense cells are binned into a shared-memory histogram
+// tile), a tile loop over all CTAs. Dense cells are binned into a shared-memory histogram
 // added to the cell's global bins; sparse cells (few keys in the bracket, known from the
-// previous pass) send their bracket keys straight to the global bins.
+// previous pass) count the keys below the bracket and send the bracket's keys to the global
+// bins (to shared bins first when there are more than a few a tile). Each CTA takes a run of
+// consecutive tiles (runs of equal length to one tile); a cell's shared bins, count below
+// and compacted keys stay with the CTA while its tiles follow one another and are added to
+// the global ones once per run.
 __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
-    __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];
     __shared__ uint32_t s_red[32];
     __shared__ float s_cmp[kCmpTile];  // a sparse tile's bracket keys, on their way to the list
     __shared__ uint32_t s_ncmp, s_base;
+    __shared__ HistCell s_hc;
+    __shared__ uint32_t s_run[2];           // the CTA's tiles [first, end)
+    __shared__ unsigned long long s_bytes;  // thread 0's count of bytes read
     if (blockIdx.x == 0 && threadIdx.x == 0) v.counters->any_active[v.pass & 1] = 0u;
     // every cell of the level finished in an earlier pass: nothing to bin
     if (v.pass > 0 && *(volatile uint32_t *)&v.counters->any_active[(v.pass - 1) & 1] == 0u) return;
-    const uint32_t total = v.tile_off[v.C];
-    unsigned long long bytes = 0;
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const TileRef tr = tile_ref(v, t);
-        if (v.state[tr.c] != kActive) continue;
-        const orb_cell_t &cell = v.heap[tr.slot];
-        const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
-        const uint32_t cell_tiles = v.tile_off[tr.c + 1] - v.tile_off[tr.c];
-        const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
-        const int K = v.hist_k[tr.c];
-        const uint32_t nb = 1u << K;
-        const int top = (int)nb - 1;
-        uint32_t *gh = v.hist + v.hist_off[tr.c];
-        if (v.listed[tr.c]) {
-            const uint32_t nread = listed_tile(v, tr, L, R, K, gh);
-            if (threadIdx.x == 0) bytes += 4ull * nread;
+    if (threadIdx.x == 0) {
+        const uint64_t total = v.tile_off[v.C];
+        s_run[0] = (uint32_t)(total * blockIdx.x / gridDim.x);
+        s_run[1] = (uint32_t)(total * (blockIdx.x + 1) / gridDim.x);
+        s_bytes = 0;
+        s_ncmp = 0;
+    }
+    __syncthreads();
+    int cur = -1;        // the cell s_hc describes (every thread follows it)
+    uint32_t below = 0;  // sparse: this thread's keys below L in the cell's tiles so far
+    // the current cell's count below L and its shared bins to the global ones
+    auto end_cell = [&]() {
+        below = block_sum(below, s_red);
+        const uint32_t mode = s_hc.mode;
+        if (threadIdx.x == 0) {
+            const uint32_t tot = below + s_hc.below;
+            if (tot) atomicAdd(&v.below[cur], tot);
+        }
+        if (mode & (kHDense | kHLocal)) {
+            const uint32_t nb = 1u << s_hc.K;
+            uint32_t *gh = s_hc.gh;
+            for (uint32_t b = threadIdx.x; b < nb; b += kThreads) {
+                const uint32_t h = s_hist[b];
+                if (h) atomicAdd(&gh[b], h);
+            }
+        }
+        if (mode & kHCompact) {
+            const uint32_t wrote = append_list(v, cur, s_cmp, &s_ncmp, &s_base);
+            if (threadIdx.x == 0) s_bytes += 4ull * wrote;
+        }
+        __syncthreads();  // s_hc and s_hist free for the next cell
+        below = 0;
+    };
+    for (uint32_t t = s_run[0]; t < s_run[1]; ++t) {
+        const int c = v.htile_cell ? (int)v.htile_cell[t] : find_cell(v.tile_off, v.C, t);
+        if (v.state[c] != kActive) continue;
+        if (c != cur) {
+            if (cur >= 0) end_cell();
+            cur = c;
+            if (threadIdx.x == 0) {
+                const int slot = level_slot(v, c);
+                const orb_cell_t &cell = v.heap[slot];
+                const uint2 rg = v.ranges[slot];
+                const uint32_t t0 = v.tile_off[c], tiles = v.tile_off[c + 1] - t0;
+                const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+                const int K = v.hist_k[c];
+                const uint32_t nb = 1u << K;
+                const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
+                uint32_t mode;
+                if (v.listed[c])
+                    mode = kHListed;
+                else if (!sparse_pass(v, c, tiles))
+                    mode = kHDense;
+                else
+                    // more than a few bracket keys a tile: shared bins first; more than a few a
+                    // bin after this pass (a further pass follows): compacted into the list
+                    mode = (v.inb[c] > kSparseGlobalKeys * tiles ? kHLocal : 0u) |
+                           (v.inb[c] > (8u << K) ? kHCompact : 0u);
+                s_hc.keys = axis_keys(v, eff_axis(cell.cutAxis));
+                s_hc.gh = v.hist + v.hist_off[c];
+                s_hc.L = L;
+                s_hc.R = R;
+                s_hc.scale = scale;
+                s_hc.K = K;
+                s_hc.mode = mode;
+                s_hc.base = rg.x;
+                s_hc.end = rg.y;
+                s_hc.t0 = t0;
+                s_hc.below = 0;
+                s_hc.gs = make_guess(L, R, scale, nb);
+            }
+            __syncthreads();
+            if (s_hc.mode & (kHDense | kHLocal)) {
+                for (uint32_t j = threadIdx.x; j < (1u << s_hc.K); j += kThreads) s_hist[j] = 0u;
+                __syncthreads();
+            }
+        }
+        const uint32_t local = t - s_hc.t0;
+        const uint32_t mode = s_hc.mode;
+        if (mode & kHListed) {
+            const uint32_t nread = listed_tile(v, c, local, &s_hc);
+            if (threadIdx.x == 0) s_bytes += 4ull * nread;
             continue;
         }
-        const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
-        const bool sparse = v.inb[tr.c] <= v.sparse_per_tile * cell_tiles;
-        // a sparse pass whose bracket still holds more than a few keys a tile bins them in
-        // shared memory first (no global atomics on the same bins from every tile)
-        const bool local = sparse && v.inb[tr.c] > kSparseGlobalKeys * cell_tiles;
-        if (!sparse || local) {
-            for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) s_hist[j] = 0u;
-            if (!sparse) fill_edges(s_edge, L, R, K, threadIdx.x, blockDim.x);
-            __syncthreads();
-        }
-        uint32_t *sbins = local ? s_hist : gh;  // where a sparse pass's bracket keys go
-        // ... and compacted into the cell's list when the bracket after this pass is still
-        // expected to hold more than a few keys a bin (so a further pass will follow)
-        const bool compact = sparse && v.inb[tr.c] > (8u << K);
-        if (compact) {
-            if (threadIdx.x == 0) s_ncmp = 0;
-            __syncthreads();
-        }
-        auto keep = [&](float k) {
-            if (!compact) return;
-            const uint32_t i = atomicAdd(&s_ncmp, 1u);
-            if (i < (uint32_t)kCmpTile) s_cmp[i] = k;
-        };
-        const float m = bin_margin(L, R, scale, nb);
-        const float one_m = __fsub_rd(1.0f, m);
-        uint32_t below = 0;
-        if (sparse) {
-            // sparse: keys below L counted, keys in [L, R) (few) binned afterwards
-            scan_tile(
-                keys, tr.e0, tr.e1, R,
+        const uint32_t e0 = s_hc.base + local * (uint32_t)kTile;
+        const uint32_t e1 = min(s_hc.end, e0 + (uint32_t)kTile);
+        const float *keys = s_hc.keys;
+        if (mode & kHDense) {
+            // the scaled guess alone, no range test (guess_bin fails keys outside [L, R)
+            // and NaN); a key it does not settle is counted in the lane's spare bin past the
+            // top (never read) and binned exactly afterwards
+            const Guess gs = s_hc.gs;
+            const uint32_t spare = (gs.lim >> 12) + (threadIdx.x & 31);
+            auto exact = [&](float k) { dense_exact(k, &s_hc, s_hist); };
+            scan_tile<kThreads>(
+                keys, e0, e1, s_hc.R,
                 [&](float k) {
-                    below += k < L;
-                    return !(k >= L && k < R);
-                },
-                [&](float k) {
-                    add_sparse(sbins, k, L, R, K);
-                    keep(k);
-                },
-                [&](float k) {
-                    if (k < L) {
-                        ++below;
-                    } else if (k < R) {
-                        add_sparse(sbins, k, L, R, K);
-                        keep(k);
-                    }
-                });
-        } else {
-            // dense: the scaled guess alone, no range test (a key below L gives a guess below
-            // bin 0 or a fraction <= m, one at or above R a guess past the top bin or a
-            // fraction >= 1 - m, NaN fails every comparison); a key it does not settle is
-            // counted in the lane's spare bin past the top (never read) and binned exactly
-            // afterwards
-            const int spare = top + 1 + (int)(threadIdx.x & 31);
-            auto exact = [&](float k) {
-                if (k < L)
-                    ++below;
-                else if (k < R)
-                    atomicAdd(&s_hist[edge_bin_slow(k, L, scale, top, s_edge)], 1u);
-            };
-            scan_tile(
-                keys, tr.e0, tr.e1, R,
-                [&](float k) {
-                    const float t = __fmul_rn(__fsub_rn(k, L), scale);
-                    const int g = __float2int_rz(t);
-                    const float f = __fsub_rn(t, __int2float_rn(g));
-                    const bool ok = g <= top && f > m && f < one_m;
+                    uint32_t g;
+                    const bool ok = guess_bin(gs, k, &g);
                     atomicAdd(&s_hist[ok ? g : spare], 1u);
                     return ok;
                 },
                 exact, exact);
+        } else {
+            // keys below L counted, keys in [L, R) (few) binned afterwards
+            const float L = s_hc.L, R = s_hc.R;
+            auto key = [&](float k) { sparse_key(k, &s_hc, s_hist, s_cmp, &s_ncmp); };
+            scan_tile<kThreads>(
+                keys, e0, e1, R,
+                [&](float k) {
+                    below += k < L;
+                    return !(k >= L && k < R);
+                },
+                key,
+                [&](float k) {
+                    if (k < L)
+                        ++below;
+                    else if (k < R)
+                        key(k);
+                });
         }
-        below = block_sum(below, s_red);
-        if (threadIdx.x == 0) {
-            if (below) atomicAdd(&v.below[tr.c], below);
-            bytes += 4ull * (tr.e1 - tr.e0);
-        }
-        if (compact) {
-            const uint32_t wrote = append_list(v, tr.c, s_cmp, s_ncmp, &s_base);
-            if (threadIdx.x == 0) bytes += 4ull * wrote;
-        }
-        if (!sparse || local) {
-            for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-                const uint32_t h = s_hist[b];
-                if (h) atomicAdd(&gh[b], h);
-            }
-            __syncthreads();
-        }
+        if (threadIdx.x == 0) s_bytes += 4ull * (e1 - e0);
     }
-    if (threadIdx.x == 0 && bytes) add_bytes(v, kKHist, bytes);
+    if (cur >= 0) end_cell();
+    if (threadIdx.x == 0 && s_bytes) add_bytes(v, kKHist, s_bytes);
 }
 
 // ------------------------------------------------------------------------------------
@@ -857,15 +973,14 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
             fill_edges(edges, L, R, K, lane, 32);
             __syncwarp();
             const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
-            const float m = bin_margin(L, R, scale, nb);
-            const float one_m = __fsub_rd(1.0f, m);
+            const Guess gs = make_guess(L, R, scale, nb);
             const int top = (int)nb - 1;
             uint32_t below = 0;
             auto one = [&](float k) {
                 if (k < L)
                     ++below;
                 else if (k < R)
-                    atomicAdd(&bins[fast_bin(k, L, scale, m, one_m, top, edges)], 1u);
+                    atomicAdd(&bins[fast_bin(k, gs, top, edges)], 1u);
             };
             visit_keys(keys, rg.x, rg.y, R, lane, 32, one, each(one));
             __syncwarp();
@@ -956,18 +1071,47 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     uint32_t prefix = v.below[c];
     uint32_t pos = 0, width = 1u << K;
     uint8_t st = kActive;
+    // The replay reads the bins through two loads: lane l first sums its run of 2^K/32 bins
+    // (the steps whose halves span whole runs add up lanes), then, once a half lies inside
+    // one run, the lanes hold that run's bins two each. No other step waits on memory.
+    const uint32_t RUN = max((1u << K) >> 5, 1u);  // bins a lane's run covers (K = 4: lanes
+                                                    // 16.. hold none)
+    uint32_t run_sum = 0;
+    if (RUN >= 4) {
+        const uint4 *g4 = reinterpret_cast<const uint4 *>(g + lane * RUN);
+#pragma unroll 4
+        for (uint32_t j = 0; j < RUN / 4; ++j) {
+            const uint4 w = g4[j];
+            run_sum += w.x + w.y + w.z + w.w;
+        }
+    } else {
+        for (uint32_t j = 0; j < RUN; ++j)
+            if (lane * RUN + j < (1u << K)) run_sum += g[lane * RUN + j];
+    }
+    uint32_t q = 0xffffffffu;  // the run whose bins the lanes hold
+    uint2 pair = make_uint2(0u, 0u);
+    // bins [a, a + w) summed over the warp (a multiple of w, w a power of two)
+    auto sum_bins = [&](uint32_t a, uint32_t w) -> uint32_t {
+        if (w >= RUN) {
+            const uint32_t l0 = a / RUN, l1 = (a + w) / RUN;
+            return warp_sum(lane >= l0 && lane < l1 ? run_sum : 0u);
+        }
+        const uint32_t r = a / RUN;
+        if (r != q) {
+            q = r;
+            const uint32_t b0 = r * RUN + 2 * lane;
+            pair.x = 2 * lane < RUN ? g[b0] : 0u;
+            pair.y = 2 * lane + 1 < RUN ? g[b0 + 1] : 0u;
+        }
+        const uint32_t b0 = q * RUN + 2 * lane;
+        return warp_sum((b0 >= a && b0 < a + w ? pair.x : 0u) + (b0 + 1 >= a && b0 + 1 < a + w ? pair.y : 0u));
+    };
     uint32_t first_half = 0xffffffffu;  // bins below the first cut, when already summed
     if (v.warm && v.warm[c]) {
-        // first pass of a hinted bracket: check it holds the target before replaying (one
-        // sweep over the bins gives the total and the first step's count)
+        // first pass of a hinted bracket: check it holds the target before replaying (the
+        // total and the first step's count)
         const uint32_t h0 = 1u << (K - 1);
-        uint32_t lo = 0, hi = 0;
-        for (uint32_t b = lane; b < h0; b += 32) {
-            lo += g[b];
-            hi += g[b + h0];
-        }
-        lo = warp_sum(lo);
-        hi = warp_sum(hi);
+        const uint32_t lo = sum_bins(0, h0), hi = sum_bins(h0, h0);
         first_half = lo;
         const bool holds = warm_bracket_holds(prefix, prefix + lo + hi, n);
         __syncwarp();
@@ -993,13 +1137,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
             break;
         }
         const uint32_t half = width >> 1;
-        uint32_t sum = 0;
-        if (step == 0 && first_half != 0xffffffffu) {
-            sum = first_half;
-        } else {
-            for (uint32_t b = lane; b < half; b += 32) sum += g[pos + b];
-            sum = warp_sum(sum);
-        }
+        const uint32_t sum = step == 0 && first_half != 0xffffffffu ? first_half : sum_bins(pos, half);
         const uint32_t cl = prefix + sum;
         ++it;
         const int dir = convergence(cl, n);
@@ -1018,11 +1156,11 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         width = half;
     }
     if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
-    const uint32_t next_inb = g[pos];  // keys in the bracket the next pass would bin
+    const uint32_t next_inb = sum_bins(pos, 1);  // keys in the bracket the next pass would bin
     // the next pass reads the cell's list when this pass read one or wrote a complete one
     // (a sparse pass compacts its bracket keys); then the keys below the new L are known
     const uint32_t tiles = v.tile_off[c + 1] - v.tile_off[c];
-    const bool list_next = v.listed[c] || (v.inb[c] <= v.sparse_per_tile * tiles &&
+    const bool list_next = v.listed[c] || (sparse_pass(v, c, tiles) &&
                                            v.inb[c] > (8u << K) && !v.cmp_bad[c]);
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
@@ -1918,15 +2056,14 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
             fill_edges(sm.edges, L, R, K, tid, blockDim.x);
             __syncthreads();
             const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
-            const float m = bin_margin(L, R, scale, nb);
-            const float one_m = __fsub_rd(1.0f, m);
+            const Guess gs = make_guess(L, R, scale, nb);
             const int top = (int)nb - 1;
             uint32_t below = 0;
             auto one = [&](float k) {
                 if (k < L)
                     ++below;
                 else if (k < R)
-                    atomicAdd(&sm.bins[fast_bin(k, L, scale, m, one_m, top, sm.edges)], 1u);
+                    atomicAdd(&sm.bins[fast_bin(k, gs, top, sm.edges)], 1u);
             };
             visit_keys<false>(keys, rg.x, rg.y, R, tid, blockDim.x, one, each(one));
             if (tid == 0) bytes += 4ull * n;
@@ -2396,7 +2533,9 @@ void launch_init(const Level &v, uint64_t n, const float lower[3], const float u
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st) {
     switch (k) {
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
-        case kKHist: k_hist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKHist:
+            k_hist<<<grid, kThreads, 0, st>>>(v);
+            break;
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
         case kKSubtreeCheck: k_subtree_check<<<1, 1024, 0, st>>>(v, arg); break;

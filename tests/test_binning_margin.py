@@ -1,8 +1,12 @@
-"""CPU check of the count pass's scaled-guess binning (k_hist, k_bisect_tile): whenever the
-guess is accepted by the margin test it is the exact leaf of the midpoint tree, i.e. the bin
-the reference's bisection descent reaches. float32 restatement of the device arithmetic; the
-margin here uses round-to-nearest (the device rounds it up), so it accepts at least as many
-guesses as the device does."""
+"""CPU check of the count pass's scaled-guess binning (guess_bin in k_hist, k_bisect_tile and
+k_subtree): whenever the guess is accepted by the margin test it is the exact leaf of the
+midpoint tree, i.e. the bin the reference's bisection descent reaches. float32 restatement of
+the device arithmetic, the fused multiply-add y = fl(fl(k-L) scale + 2^11) rounded once (exact
+products in float64, rational arithmetic where the float64 sum is inexact); the margin here
+uses round-to-nearest (the device rounds it up), so it accepts at least as many guesses as
+the device does."""
+from fractions import Fraction
+
 import numpy as np
 
 f32 = np.float32
@@ -29,24 +33,63 @@ def margin(L, R, scale, nb):
     return f32(f32(f32(8.0) * u) * scale) + f32(f32(nb) * f32(2.0 ** -21))
 
 
+def _round_f32(q: Fraction) -> np.float32:
+    """q rounded to the nearest float32, ties to even (q inside the float32 range)."""
+    c = f32(float(q))
+    best = None
+    for cand in (np.nextafter(c, f32(-np.inf)), c, np.nextafter(c, f32(np.inf))):
+        dist = abs(Fraction(float(cand)) - q)
+        key = (dist, int(np.array(cand, f32).view(np.uint32)) & 1)
+        if best is None or key < best[0]:
+            best = (key, cand)
+    return f32(best[1])
+
+
+def fma_2048(a, scale):
+    """float32 fl(a * scale + 2048) rounded once, for float32 arrays a and scalar scale."""
+    p = a.astype(np.float64) * np.float64(scale)  # exact: 24 x 24 bits
+    s = p + 2048.0
+    y = s.astype(f32)
+    inexact = np.isfinite(p) & ((s - 2048.0) != p)
+    for i in np.nonzero(inexact)[0]:
+        y[i] = _round_f32(Fraction(float(a[i])) * Fraction(float(scale)) + 2048)
+    return y
+
+
+def guess_bin(k, L, R, scale, nb):
+    """(ok, bin) of the device's guess_bin over keys k."""
+    M = f32(margin(L, R, scale, max(nb, 2048)) * f32(4096.0))
+    if M < 2048:
+        mi = int(M)
+        span = 4095 - 2 * mi
+    else:
+        mi, span = 0, 0
+    base = int(np.array(2048.0, f32).view(np.uint32)) + mi + 1
+    y = fma_2048((k - f32(L)).astype(f32), scale)
+    e = (y.view(np.uint32).astype(np.int64) - base) & 0xFFFFFFFF
+    ok = (e < (nb << 12)) & ((e & 0xFFF) < span)
+    return ok, e >> 12
+
+
 def check_bracket(rng, L, R, K, nkeys):
     nb = 1 << K
     e = midpoint_edges(L, R, K)
     scale = f32(nb) / f32(R - L)
-    m = margin(L, R, scale, nb)
-    one_m = f32(1.0) - m
     # keys: uniform in [L, R), plus edges and their float neighbours
     k = (f32(L) + f32(R - L) * rng.random(nkeys).astype(f32)).astype(f32)
     j = rng.integers(0, nb + 1, nkeys // 4)
     near = np.concatenate([e[j], np.nextafter(e[j], f32(np.inf)), np.nextafter(e[j], f32(-np.inf))])
     k = np.concatenate([k, near.astype(f32)])
     k = k[(k >= L) & (k < R)]
-    t = (k - f32(L)).astype(f32) * scale
-    g = np.trunc(t).astype(np.int64)
-    fr = (t - g.astype(f32)).astype(f32)
-    ok = (g <= nb - 1) & (fr > m) & (fr < one_m)
     exact = np.searchsorted(e[:nb], k, side="right") - 1  # largest b with e[b] <= k
+    ok, g = guess_bin(k, L, R, scale, nb)
     bad = ok & (g != exact)
+    # keys outside [L, R) (neighbours of the end edges, NaN) are never accepted
+    out = np.concatenate([np.nextafter(np.array([L, L], f32), f32(-np.inf)), np.array([R], f32),
+                          np.nextafter(np.array([R], f32), f32(np.inf)),
+                          np.array([np.nan, np.inf, -np.inf], f32)])
+    ok_out, _ = guess_bin(out, L, R, scale, nb)
+    assert not ok_out.any(), f"key outside [{L!r}, {R!r}) accepted"
     return int(ok.sum()), int(bad.sum()), len(k)
 
 
@@ -86,8 +129,6 @@ def test_guess_settles_almost_every_key_of_a_box():
     L, R, K = f32(-0.5), f32(0.5), 11
     nb = 1 << K
     scale = f32(nb) / f32(R - L)
-    m = margin(L, R, scale, nb)
     k = (L + f32(R - L) * rng.random(200000).astype(f32)).astype(f32)
-    t = (k - L).astype(f32) * scale
-    fr = (t - np.trunc(t).astype(f32)).astype(f32)
-    assert ((fr > m) & (fr < f32(1.0) - m)).mean() > 0.99
+    ok, _ = guess_bin(k, L, R, scale, nb)
+    assert ok.mean() > 0.99
