@@ -405,7 +405,7 @@ def gpu_arm(args):
     t0 = time.perf_counter()
     if args.tuning:
         names = ("hist_blocks_per_sm", "part_blocks_per_sm", "tile_blocks_per_sm",
-                 "sparse_keys_per_tile", "cta_min_cells", "subtree_levels")
+                 "sparse_keys_per_tile", "cta_min_cells", "subtree_levels", "predict_sigmas")
         ctx.set_tuning(**dict(zip(names, (int(v) for v in args.tuning.split(",")))))
         tuning, tuned_by = ctx.get_tuning(), "--tuning"
     else:
@@ -531,6 +531,19 @@ def gpu_arm(args):
         "share_of_kernel_time": round(dom_share, 4),
     }
     wsteps = max(args.warmup, 1)
+    # count-left (the spec kernel family): every launch that counts keys below a cut in
+    # the warm-up steps, against the measured HBM peak; the last levels run inside k_subtree
+    # (bisection and partition of one cell per CTA), listed in kernels_per_step_warmup
+    cl_names = [k for k in ("count_left_hist", "bisect_tile", "bisect_warp", "count_left_sample",
+                            "count_left_sample_pick") if k in warm]
+    cl_bytes = sum(warm[k]["bytes"] for k in cl_names) / wsteps
+    cl_ms = sum(warm[k]["total_ms"] for k in cl_names) / wsteps
+    cl_gbs = cl_bytes / (cl_ms / 1e3) / 1e9 if cl_ms else None
+    count_left = {"kernels": cl_names, "bytes_per_step": cl_bytes, "ms_per_step": round(cl_ms, 4),
+                  "achieved": round(cl_gbs, 1) if cl_gbs else None, "peak": peak, "unit": "GB/s",
+                  "frac": round(cl_gbs / peak, 4) if cl_gbs else None,
+                  "peak_source": f"{peak_kind} hbm_gbs",
+                  "bytes": "4 B per key read + 4 B per key compacted (algorithmic, engine counters)"}
     kernels = {k: {"launches": v["launches"] // wsteps,
                    "ms": round(v["total_ms"] / wsteps, 4),
                    "GBps": round(v["bytes"] / (v["total_ms"] / 1e3) / 1e9, 1) if v["total_ms"] else None}
@@ -572,6 +585,7 @@ def gpu_arm(args):
                 "call": "orb_build(x,y,z host pinned, perm=NULL): reordered x,y,z + heap + ranges back",
                 "ms_per_step": 1e3 * e2e_s / len(e2e_times)},
         "roofline": roofline,
+        "count_left": count_left,
         "kernels_per_step_warmup": kernels,
         "gpu_launches": launches,
         "cpu_baseline": cpu,
@@ -599,7 +613,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--tuning", default=None,
-                    help="hist,part,tile,sparse,cta,subtree: use this launch tuning for the headline "
+                    help="hist,part,tile,sparse,cta,subtree[,predict]: use this launch tuning for the headline "
                          "instead of autotuning it (profiling runs reuse a chosen setting)")
     args = ap.parse_args()
     if args.impl == "reference":

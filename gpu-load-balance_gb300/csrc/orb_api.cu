@@ -73,9 +73,9 @@ struct orb_ctx {
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint32_t> htile_cell, ptile_cell;
     // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
-    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 3u};
+    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 3u, 0u};
     DevBuf<uint8_t> hist_k, state, iters, listed, cmp_bad;
-    DevBuf<uint32_t> cmp_off, cmp_cnt;
+    DevBuf<uint32_t> cmp_off, cmp_cnt, pred;
     DevBuf<float> cmp_keys;
     DevBuf<uint32_t> hist;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
@@ -187,8 +187,9 @@ orb_status ensure_level_buffers(orb_ctx *ctx, uint64_t n, uint32_t max_cells, ui
     ORB_CUDA(ctx->cmp_bad.ensure(max_cells));
     ORB_CUDA(ctx->cmp_off.ensure(max_cells + 1));
     ORB_CUDA(ctx->cmp_cnt.ensure(max_cells));
-    // compaction lists: n/16 per cell of more than one tile, at least 2048 (list_capacity)
-    ORB_CUDA(ctx->cmp_keys.ensure(n / 16 + 2048ull * (n / kTile + 1) + 16));
+    ORB_CUDA(ctx->pred.ensure(max_cells));
+    // compaction lists: n/8 per cell of more than one tile, at least 2048 (list_capacity)
+    ORB_CUDA(ctx->cmp_keys.ensure(n / 8 + 2048ull * (n / kTile + 1) + 16));
     ORB_CUDA(ctx->slots.ensure(max_cells));
     ORB_CUDA(ctx->hist.ensure(max_bins, true));
     ORB_CUDA(ctx->ptile_off.ensure(max_cells + 1));
@@ -218,6 +219,8 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.cmp_off = ctx->cmp_off.p;
     v.cmp_cnt = ctx->cmp_cnt.p;
     v.cmp_keys = ctx->cmp_keys.p;
+    v.pred = ctx->pred.p;
+    v.pred_sigmas = (float)ctx->tune.predict_sigmas;
     v.hist = ctx->hist.p;
     v.below = ctx->below.p;
     v.inb = ctx->inb.p;
@@ -391,12 +394,13 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
                           (const void *)v.pt_ge_pre, (const void *)v.pt_le_pre, (const void *)v.pt_status,
                           (const void *)v.part_s, (const void *)v.part_i, (const void *)v.part_le,
-                          (const void *)v.counters})
+                          (const void *)v.pred, (const void *)v.counters})
         key_add(key, p);
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
     for (uint32_t t : {ctx->tune.hist_blocks_per_sm, ctx->tune.part_blocks_per_sm, ctx->tune.tile_blocks_per_sm,
-                       ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells, ctx->tune.subtree_levels})
+                       ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells, ctx->tune.subtree_levels,
+                       ctx->tune.predict_sigmas})
         key.push_back(t);
     return key;
 }
@@ -416,10 +420,13 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
 // Bisection of every cell of the level to completion (found or capped): a fixed number of
 // histogram/resolve passes, with no host round trip (a pass after the level is done exits
 // at once on the device).
-orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes) {
+// first: the count pass the first pass uses: 1 every cell dense (a cold level without
+// sampled brackets), 2 a sampled level, 0 the general one (warm builds).
+orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes, int first) {
     for (int pass = 0; pass < kHistPasses; ++pass) {
         v.pass = pass;
-        run_kernel(ctx, kKHist, v, ctx->num_sms * (int)ctx->tune.hist_blocks_per_sm);
+        run_kernel(ctx, kKHist, v, ctx->num_sms * (int)ctx->tune.hist_blocks_per_sm,
+                   pass == 0 ? first : 0);
         run_kernel(ctx, kKResolve, v, pass_grid(ctx));
         ++*passes;
     }
@@ -456,8 +463,10 @@ int subtree_from(const orb_ctx *ctx, const std::vector<LevelDesc> &lv, uint64_t 
 // sub_from >= 0: from level lv[sub_from] down, one CTA per cell finishes the tree when every
 // cell of that level fits one (k_subtree_check decides on the device); the level kernels of
 // those levels then return at once.
+// max_n: the largest instance's particles (cells of level l hold about max_n >> l); levels
+// whose cells can be large enough get a sampled first count pass (k_sample_bin, k_sample_pick).
 orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes,
-                      int sub_from = -1) {
+                      int sub_from, uint64_t max_n) {
     for (size_t li = 0; li < lv.size(); ++li) {
         const LevelDesc &d = lv[li];
         v.base = d.base;
@@ -476,9 +485,17 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
             // many cells: one CTA bisects one cell, no host round trip
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
         } else {
+            // cold levels with cells of at least 2^18 particles: sampled brackets for the
+            // first count pass (decided per cell on the device; result-invariant)
+            const bool sampled =
+                !v.hint && ctx->tune.predict_sigmas && (max_n >> li) + 8ull * li >= (1ull << 18);
+            if (sampled) {
+                run_kernel(ctx, kKSample, v, 0);
+                run_kernel(ctx, kKSamplePick, v, 0);
+            }
             run_kernel(ctx, kKBisectWarp, v, 1);  // cells small enough for one warp
             run_kernel(ctx, kKBisectTile, v, std::min(v.C, ctx->num_sms * (int)ctx->tune.tile_blocks_per_sm));
-            orb_status st = run_bisection(ctx, v, passes);
+            orb_status st = run_bisection(ctx, v, passes, v.hint ? 0 : (sampled ? 2 : 1));
             if (st != ORB_OK) return st;
         }
         partition_level(ctx, v, true);
@@ -676,7 +693,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         ctx->launches[kKInit] += 1;
         launch_init(v, n, lower, upper, d, (int)heap_cells, s);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp, sub_from);
+        return run_levels(ctx, v, lv, pp, sub_from, n);
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
@@ -719,6 +736,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         info->d2h_ms = d2h_ms;
         info->warm_cells = ctx->h_counters->warm_cells;
         info->warm_resets = ctx->h_counters->warm_resets;
+        info->sampled_cells = ctx->h_counters->pred_cells;
+        info->sampled_misses = ctx->h_counters->pred_misses;
     }
     return ORB_OK;
 }
@@ -1147,7 +1166,7 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
         ctx->launches[kKInit] += 1;
         launch_init_batch(v, ctx->batch_roots.p, (int)k, n_total, s);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp, sub_from);
+        return run_levels(ctx, v, lv, pp, sub_from, max_n);
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
@@ -1203,6 +1222,8 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
         info->d2h_ms = d2h_ms;
         info->warm_cells = ctx->h_counters->warm_cells;
         info->warm_resets = ctx->h_counters->warm_resets;
+        info->sampled_cells = ctx->h_counters->pred_cells;
+        info->sampled_misses = ctx->h_counters->pred_misses;
     }
     return ORB_OK;
 }
@@ -1261,7 +1282,8 @@ static bool tuning_valid(const orb_tuning &t) {
     return t.hist_blocks_per_sm >= 1 && t.hist_blocks_per_sm <= 8 &&
            t.part_blocks_per_sm >= 1 && t.part_blocks_per_sm <= 16 && t.tile_blocks_per_sm >= 1 &&
            t.tile_blocks_per_sm <= 8 && t.sparse_keys_per_tile >= 1 &&
-           t.sparse_keys_per_tile <= (uint32_t)kTile && t.subtree_levels <= (uint32_t)kSubMaxLevels;
+           t.sparse_keys_per_tile <= (uint32_t)kTile && t.subtree_levels <= (uint32_t)kSubMaxLevels &&
+           t.predict_sigmas <= 16;
 }
 
 orb_status orb_set_tuning(orb_ctx *ctx, const orb_tuning *t) {
@@ -1343,7 +1365,7 @@ orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, cons
     // coordinate descent over result-invariant parameters
     static const uint32_t hist_c[] = {4, 6, 8}, part_c[] = {4, 8, 16}, tile_c[] = {2, 4},
                           sparse_c[] = {16, 64, 256}, cta_c[] = {0, 512, 4096},
-                          sub_c[] = {0, 2, 3, 4, 6};
+                          sub_c[] = {0, 2, 3, 4, 6}, pred_c[] = {0, 4, 5, 7};
     struct Axis {
         uint32_t orb_tuning::*field;
         const uint32_t *vals;
@@ -1354,7 +1376,8 @@ orb_status orb_autotune_batch(orb_ctx *ctx, const float *x, const float *y, cons
                          {&orb_tuning::tile_blocks_per_sm, tile_c, 2},
                          {&orb_tuning::sparse_keys_per_tile, sparse_c, 3},
                          {&orb_tuning::cta_min_cells, cta_c, 3},
-                         {&orb_tuning::subtree_levels, sub_c, 5}};
+                         {&orb_tuning::subtree_levels, sub_c, 5},
+                         {&orb_tuning::predict_sigmas, pred_c, 4}};
     for (const Axis &ax : axes) {
         const orb_tuning base = cur;
         for (int i = 0; i < ax.n; ++i) {

@@ -20,7 +20,11 @@ constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass
 // (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
 constexpr int kHistPasses = 4;
 constexpr int kThreads = 256;
-constexpr int kHistBlocksPerSm = 8;  // resident CTAs of the count-left pass (most useful grid)
+// resident CTAs of the count-left pass (its launch bound: 65536 / (256 x 6) = 40 registers)
+#ifndef ORB_HIST_BLOCKS_PER_SM
+#define ORB_HIST_BLOCKS_PER_SM 6
+#endif
+constexpr int kHistBlocksPerSm = ORB_HIST_BLOCKS_PER_SM;
 constexpr int kTileBlocksPerSm = 4;  // resident CTAs of the one-tile cell bisection
 constexpr int kSubtreeBlocksPerSm = 4;  // CTAs of the subtree kernel per SM (its grid)
 constexpr uint32_t kSubMaxParticles = 17408;  // largest cell one subtree CTA takes
@@ -50,6 +54,8 @@ enum Kernel : int {
     kKWarmStart,
     kKSubtreeCheck,
     kKSubtree,
+    kKSample,
+    kKSamplePick,
     kNumKernels
 };
 static_assert(kNumKernels <= 32, "BuildCounters::bytes holds 32 kernel kinds");
@@ -66,6 +72,8 @@ struct BuildCounters {
     uint32_t ticket;      // block ticket of the tile scan (reset before each launch)
     uint32_t warm_cells;  // warm builds: cells that started from a hinted bracket
     uint32_t warm_resets; // ... whose hinted bracket missed the target (restarted cold)
+    uint32_t pred_cells;  // cells whose first count pass used a sampled bracket
+    uint32_t pred_misses; // ... whose sampled bracket did not hold the cut (binned again)
     unsigned long long bytes[32];  // algorithmic bytes per Kernel kind
 };
 
@@ -98,6 +106,11 @@ struct Level {
     float *cmp_keys;        // the lists
     uint8_t *listed;        // [C]   1: this pass reads the cell's list instead of its keys
     uint8_t *cmp_bad;       // [C]   1: a tile's bracket keys overflowed (no list)
+    // sampled first pass: leaves [lo, hi) of the first pass's midpoint tree predicted to hold
+    // the cut (k_sample_bin, k_sample_pick); that pass counts the keys below leaf lo and bins
+    // only the keys of [lo, hi). Packed (lo | hi << 12 | flags); 0: no prediction (dense)
+    uint32_t *pred;         // [C]
+    float pred_sigmas;      // half-width of the sampled bracket in standard errors (0: off)
     // partition
     uint32_t *ptile_off;    // [C+1] first partition tile of each cell
     uint32_t *ge_bits;      // [ptiles * kPWords] bit p: key >= cut

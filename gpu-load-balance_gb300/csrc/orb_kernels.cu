@@ -24,7 +24,8 @@ namespace orb {
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
-    "tile_map", "bisect_warp", "bisect_tile", "warm_start", "subtree_check", "subtree"};
+    "tile_map", "bisect_warp", "bisect_tile", "warm_start", "subtree_check", "subtree",
+    "count_left_sample", "count_left_sample_pick"};
 
 namespace {
 
@@ -199,9 +200,11 @@ __device__ __forceinline__ TileRef tile_ref(const Level &v, uint32_t t) {
 }
 
 // Capacity of a cell's compaction list: cells the histogram passes bisect (more than one
-// tile) get n/16 keys, at least 2048 (16x the sparse threshold's bracket).
+// tile) get n/8 keys, at least 2048 (16x the sparse threshold's bracket): room for the
+// sampled bracket of a first pass (at most kPredCompactShare of the keys) and for the
+// bracket of a sparse pass.
 __host__ __device__ __forceinline__ uint32_t list_capacity(uint32_t n) {
-    return n > (uint32_t)kTile ? (n / 16 > 2048u ? n / 16 : 2048u) : 0u;
+    return n > (uint32_t)kTile ? (n / 8 > 2048u ? n / 8 : 2048u) : 0u;
 }
 
 __device__ __forceinline__ int tree_depth(uint32_t n) {
@@ -438,6 +441,22 @@ __device__ __forceinline__ int tree_bin(float k, float L, float R, int K) {
     return b;
 }
 
+// Edge e(j) of that tree (e(0) = L, e(2^K) = R): the lower end of leaf j, reached by the same
+// midpoints as tree_bin. The edges are non-decreasing (a midpoint of [lo, hi] rounds into
+// [lo, hi]), so tree_bin(k) >= j exactly when k >= e(j), for L <= k < R.
+__device__ __forceinline__ float tree_edge(float L, float R, int K, uint32_t j) {
+    if (j >= (1u << K)) return R;
+    float lo = L, hi = R;
+    for (int d = K - 1; d >= 0; --d) {
+        const float mm = mid_cut(lo, hi);
+        if (j & (1u << d))
+            lo = mm;
+        else
+            hi = mm;
+    }
+    return lo;
+}
+
 // Bin of key k (L <= k < R) in the edge table e[0..nb]: the largest b with e[b] <= k, i.e.
 // the leaf the bisection's descent reaches. The spacing of the edges is uniform to a few
 // ulps, so the scaled guess is off by at most one except in brackets only a few ulps
@@ -521,6 +540,23 @@ __device__ __forceinline__ bool guess_bin(const Guess &g, float k, uint32_t *b) 
     return e < g.lim && (e & 0xfffu) < g.span;
 }
 
+// Exact bin of L <= k < R by the edge table e[0..top+1] (in shared memory) for a key the
+// scaled guess did not settle: floor(t) of the same guess, then its neighbours (the guess is
+// off by at most one bin when the margin lets it be trusted at all: bins are then more than
+// 16 ulps wide); a search over the table otherwise (out of line: brackets a few ulps wide).
+__device__ __forceinline__ uint32_t near_bin(float k, const Guess &gs, const float *e, uint32_t top) {
+    const uint32_t t = __float_as_uint(__fmaf_rn(__fsub_rn(k, gs.L), gs.scale, 2048.0f)) - 0x45000000u;
+    const uint32_t g = min(t >> 12, top);  // 0x45000000: the encoding of 2048.0f (t >= 0 for k >= L)
+    if (k < e[g]) {
+        if (g > 0 && !(k < e[g - 1])) return g - 1;
+    } else if (!(k < e[g + 1])) {
+        if (g < top && k < e[g + 2]) return g + 1;
+    } else {
+        return g;
+    }
+    return (uint32_t)edge_bin_slow(k, gs.L, gs.scale, (int)top, e);
+}
+
 // edge_bin() with the guess accepted outright when guess_bin() proves it; L <= k < R.
 __device__ __forceinline__ int fast_bin(float k, const Guess &g, int top, const float *e) {
     uint32_t b;
@@ -530,38 +566,43 @@ __device__ __forceinline__ int fast_bin(float k, const Guess &g, int top, const 
 
 
 
-// One bracket key of a sparse pass into the cell's bins (global, or shared for a sparse
-// pass whose bracket holds more than kSparseGlobalKeys keys a tile), out of line as above.
+// A sparse pass sends its bracket keys to the cell's global bins, or to shared bins first
+// when its bracket holds more than kSparseGlobalKeys keys a tile.
 constexpr uint32_t kSparseGlobalKeys = 8;
-constexpr int kCmpTile = 1024;  // bracket keys a CTA compacts for one cell's run of tiles (more:
-                                // the cell keeps no list)
+constexpr int kCmpTile = 2048;  // bracket keys a CTA compacts for one cell's run of tiles, or
+                                // for one tile of a sampled pass (more: the cell keeps no list)
 
 // The cell a count pass's CTA is working on, in shared memory (thread 0 fills it when the
-// CTA's tiles move to a new cell): the out-of-line paths read it there, so the streaming loop
-// keeps only what it needs in registers.
-constexpr uint32_t kHDense = 1, kHLocal = 2, kHCompact = 4, kHListed = 8;
+// CTA's tiles move to a new cell): the rare paths read it there, so the streaming loop keeps
+// only what it needs in registers.
+constexpr uint32_t kHDense = 1, kHLocal = 2, kHCompact = 4, kHListed = 8, kHPred = 16;
 struct HistCell {
     const float *keys;  // the cut axis
     uint32_t *gh;       // the cell's global bins
     float L, R, scale;
     int K;
-    uint32_t mode;      // kHDense, else sparse (kHLocal: bracket keys to shared bins first;
+    uint32_t mode;      // kHDense, kHPred (sampled bracket; kHCompact: its keys to the
+                        // list), else sparse (kHLocal: bracket keys to shared bins first;
                         // kHCompact: and to the list), or kHListed
     uint32_t base, end; // the cell's key range [base, end)
     uint32_t t0;        // its first tile
     uint32_t below;     // dense: keys below L met by the exact path
-    Guess gs;           // dense: the scaled guess
+    float pa, pb;       // kHPred: the sampled bracket [e(lo), e(hi)) of the tree over [L, R)
+    Guess gs;           // dense and kHPred: the scaled guess
 };
 
-// Count pass over a cell whose bracket keys an earlier pass compacted: tile j of the cell
-// takes list keys [j kTile, (j+1) kTile) and bins those inside [L, R) (the keys below L are
-// already counted: resolve carried them). Returns the keys read.
+// Count pass over a cell whose bracket keys an earlier pass compacted: tile j of the cell's
+// t tiles takes the j-th of t equal runs of the list and bins its keys inside [L, R) (the
+// keys below L are already counted: resolve carried them). Returns the keys read.
 __device__ __noinline__ uint32_t listed_tile(const Level &v, int c, uint32_t local, const HistCell *hc) {
     const float L = hc->L, R = hc->R;
     const int K = hc->K;
     uint32_t *gh = hc->gh;
     const uint32_t cnt = v.cmp_cnt[c];
-    const uint32_t lo = local * (uint32_t)kTile, hi = min(cnt, lo + (uint32_t)kTile);
+    // the list split evenly over the cell's tiles, so the CTAs of all of them share it
+    const uint32_t tiles = v.tile_off[c + 1] - v.tile_off[c];
+    const uint32_t chunk = (cnt + tiles - 1) / tiles;
+    const uint32_t lo = local * chunk, hi = min(cnt, lo + chunk);
     const float *list = v.cmp_keys + v.cmp_off[c];
     for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const float k = list[i];
@@ -606,7 +647,7 @@ __device__ __noinline__ uint32_t append_list(const Level &v, int c, const float 
 
 // A sparse pass's bracket key (L <= k < R): into the cell's bins (shared when kHLocal) and,
 // with kHCompact, into the tile's list buffer.
-__device__ __noinline__ void sparse_key(float k, const HistCell *hc, uint32_t *s_hist, float *s_cmp,
+__device__ __forceinline__ void sparse_key(float k, const HistCell *hc, uint32_t *s_hist, float *s_cmp,
                                         uint32_t *s_ncmp) {
     const uint32_t mode = hc->mode;
     const uint32_t b = (uint32_t)tree_bin(k, hc->L, hc->R, hc->K);
@@ -618,13 +659,34 @@ __device__ __noinline__ void sparse_key(float k, const HistCell *hc, uint32_t *s
 }
 
 // A dense pass's key the scaled guess did not settle: below L counted, inside [L, R) binned
-// by the reference's descent (tree_bin), at or past R (or NaN) ignored.
-__device__ __noinline__ void dense_exact(float k, HistCell *hc, uint32_t *s_hist) {
+// by the edge table (near_bin), at or past R (or NaN) ignored.
+__device__ __forceinline__ void dense_exact(float k, HistCell *hc, uint32_t *s_hist, const float *s_edge) {
     const float L = hc->L, R = hc->R;
     if (k < L)
         atomicAdd(&hc->below, 1u);
     else if (k < R)
-        atomicAdd(&s_hist[tree_bin(k, L, R, hc->K)], 1u);
+        atomicAdd(&s_hist[near_bin(k, hc->gs, s_edge, (1u << hc->K) - 1u)], 1u);
+}
+
+// A sampled pass's bracket key (e(lo) <= k < e(hi), inside [L, R)): its bin by the scaled
+// guess (the edge table when the guess is not proven) into the shared bins and,
+// when the pass compacts, into the tile's list buffer (one shared reservation for the
+// threads that arrive together).
+__device__ __noinline__ void pred_key(float k, const HistCell *hc, uint32_t *s_hist, float *s_cmp,
+                                      uint32_t *s_ncmp, const float *s_edge) {
+    uint32_t g;
+    if (!guess_bin(hc->gs, k, &g)) g = near_bin(k, hc->gs, s_edge, (1u << hc->K) - 1u);
+    atomicAdd(&s_hist[g], 1u);
+    if (hc->mode & kHCompact) {
+        const uint32_t m = __activemask();
+        const uint32_t lane = threadIdx.x & 31u;
+        const uint32_t leader = (uint32_t)__ffs(m) - 1u;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(s_ncmp, (uint32_t)__popc(m));
+        base = __shfl_sync(m, base, (int)leader);
+        const uint32_t i = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        if (i < (uint32_t)kCmpTile) s_cmp[i] = k;
+    }
 }
 
 // A compile-time flag passed to a generic lambda.
@@ -639,29 +701,36 @@ constexpr int kHistVec = 4;
 constexpr int kGroup = 4 * kHistVec;  // keys a thread holds per round
 
 // The keys [e0, e1) of one tile (at most kTile keys), visited by the CTA's threads. The
-// float4 body goes through settle(k, i) (i = the key's slot in its round), branch-free code
-// that handles the common case and returns false for a key it leaves; those are remembered
-// by one bit each and visited afterwards through rest(k), and the unaligned head and tail
-// through visit(k). `pad` fills the body's missing lanes: settle(pad) must count nothing
-// (a pad it leaves is skipped by the walk).
+// 16-byte aligned body is read in rounds of kHistVec float4 loads a thread (all issued
+// before any key is used); each key goes through settle(k), branch-free code for the common
+// case that returns false for a key it leaves. Left keys are visited through rest(k)
+// (reloaded): after the tile's last round, from one bit each (Rounds = false: for passes
+// that leave few keys), or right after their own round while its lines are still in L1
+// (Rounds = true: for passes that leave a few percent). The unaligned head and tail go
+// through visit(k). `pad` fills the missing lanes of the last round: settle(pad) must count
+// nothing (a pad it leaves is skipped).
 static_assert(kTile / (4 * kHistVec * kThreads) <= 4, "scan_tile keeps 16 bits a round, 4 rounds");
-template <uint32_t NT, class Settle, class Rest, class Visit>
+template <uint32_t NT, bool Rounds, class Settle, class Rest, class Visit>
 __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32_t e1, float pad,
                                           Settle settle, Rest rest, Visit visit) {
-    const uint32_t ti = threadIdx.x, nt = NT;  // NT = blockDim.x
+    const uint32_t ti = threadIdx.x;  // NT = blockDim.x
     const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
     const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
-    for (uint32_t i = e0 + ti; i < a0; i += nt) visit(__ldg(keys + i));
+    for (uint32_t i = e0 + ti; i < a0; i += NT) visit(__ldg(keys + i));
     const uint32_t n4 = (e1 - a0) >> 2;
     const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
-    unsigned long long left = 0;  // bit 16 r + 4 u + c: component c of load u of round r
+    const float *kb = keys + a0;
+    unsigned long long left = 0;  // Rounds = false: bit 16 r + 4 u + c: component c of load u
     uint32_t r = 0, j0 = 0;
-    // one round: kHistVec float4 loads in flight, then the 16 keys; Full: every load in range
+    auto take = [&](uint32_t b, uint32_t jr) {  // bit b of round jr
+        const uint32_t j = jr + ((b >> 2) & 3u) * NT + ti;
+        if (j < n4) rest(__ldg(kb + 4 * j + (b & 3u)));  // else a pad lane
+    };
     auto round = [&](auto full) {
         float4 q[kHistVec];
 #pragma unroll
         for (int u = 0; u < kHistVec; ++u) {
-            const uint32_t j = j0 + u * nt + ti;
+            const uint32_t j = j0 + u * NT + ti;
             if (decltype(full)::value)
                 q[u] = __ldg(k4 + j);
             else
@@ -674,17 +743,24 @@ __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32
 #pragma unroll
             for (int c = 0; c < 4; ++c) miss |= (uint32_t)!settle(kk[c]) << (4 * u + c);
         }
-        left |= (unsigned long long)miss << (16u * r);
+        if (Rounds) {
+            while (miss) {
+                const uint32_t b = (uint32_t)__ffs(miss) - 1u;
+                miss &= miss - 1u;
+                take(b, j0);
+            }
+        } else {
+            left |= (unsigned long long)miss << (16u * r);
+        }
     };
-    for (; j0 + kHistVec * nt <= n4; j0 += kHistVec * nt, ++r) round(Flag<true>());
+    for (; j0 + kHistVec * NT <= n4; j0 += kHistVec * NT, ++r) round(Flag<true>());
     if (j0 < n4) round(Flag<false>());
     while (left) {
-        const int b = __ffsll((long long)left) - 1;
+        const uint32_t b = (uint32_t)(__ffsll((long long)left) - 1);
         left &= left - 1;
-        const uint32_t j = (uint32_t)(b >> 4) * (kHistVec * nt) + (uint32_t)((b >> 2) & 3) * nt + ti;
-        if (j < n4) rest(__ldg(keys + a0 + 4 * j + (b & 3)));  // else a pad lane
+        take(b, (b >> 4) * (kHistVec * NT));
     }
-    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(__ldg(keys + i));
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += NT) visit(__ldg(keys + i));
 }
 
 // Group visitor that applies a per-key visitor to each key in order.
@@ -732,11 +808,275 @@ __device__ __forceinline__ void visit_keys(const float *keys, uint32_t e0, uint3
     for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += nt) visit(ld(keys + i));
 }
 
+// The dense pass's tile [e0, e1) in the first pass of a cold level: every key binned by the
+// scaled guess into the CTA's shared bins (a key the guess does not settle counted in the
+// lane's spare bin and binned exactly right after its round). Rounds of kHistVec float4
+// loads a thread; the unaligned head and tail and a last partial round key by key.
+__device__ __forceinline__ void dense_tile(const float *keys, uint32_t e0, uint32_t e1, const Guess gs,
+                                           uint32_t *s_hist, HistCell *hc, const float *s_edge) {
+    const uint32_t ti = threadIdx.x;
+    const uint32_t spare = (gs.lim >> 12) + (ti & 31u);
+    auto one = [&](float k) {
+        uint32_t g;
+        if (guess_bin(gs, k, &g))
+            atomicAdd(&s_hist[g], 1u);
+        else
+            dense_exact(k, hc, s_hist, s_edge);
+    };
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
+    const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
+    for (uint32_t i = e0 + ti; i < a0; i += kThreads) one(__ldg(keys + i));
+    const uint32_t n4 = (e1 - a0) >> 2;
+    const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
+    const float *kb = keys + a0;
+    uint32_t j0 = 0;
+#pragma unroll 1
+    for (; j0 + kHistVec * kThreads <= n4; j0 += kHistVec * kThreads) {
+        float4 q[kHistVec];
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) q[u] = __ldg(k4 + j0 + u * kThreads + ti);
+        uint32_t miss = 0;
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            const float kk[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                uint32_t g;
+                const bool ok = guess_bin(gs, kk[c], &g);
+                atomicAdd(&s_hist[ok ? g : spare], 1u);
+                if (!ok) miss |= 1u << (4 * u + c);
+            }
+        }
+        while (miss) {
+            const uint32_t b = (uint32_t)__ffs(miss) - 1u;
+            miss &= miss - 1u;
+            dense_exact(__ldg(kb + 4 * (j0 + (b >> 2) * kThreads + ti) + (b & 3u)), hc, s_hist, s_edge);
+        }
+    }
+    for (uint32_t j = j0 + ti; j < n4; j += kThreads) {
+        const float4 q = __ldg(k4 + j);
+        one(q.x);
+        one(q.y);
+        one(q.z);
+        one(q.w);
+    }
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += kThreads) one(__ldg(keys + i));
+}
+
+// A sparse pass's tile [e0, e1): keys below L counted in `below`, keys inside [L, R) (a few a
+// tile) handed to key(k) right after their round, keys at or above R and NaN ignored. Same
+// rounds as dense_tile.
+template <class Key>
+__device__ __forceinline__ void sparse_tile(const float *keys, uint32_t e0, uint32_t e1, float L, float R,
+                                            uint32_t &below, Key key) {
+    const uint32_t ti = threadIdx.x;
+    auto one = [&](float k) {
+        if (k < L)
+            ++below;
+        else if (k < R)
+            key(k);
+    };
+    const uintptr_t addr = reinterpret_cast<uintptr_t>(keys + e0);
+    const uint32_t a0 = min(e1, e0 + (uint32_t)(((16u - (addr & 15u)) & 15u) >> 2));
+    for (uint32_t i = e0 + ti; i < a0; i += kThreads) one(__ldg(keys + i));
+    const uint32_t n4 = (e1 - a0) >> 2;
+    const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
+    const float *kb = keys + a0;
+    uint32_t j0 = 0;
+#pragma unroll 1
+    for (; j0 + kHistVec * kThreads <= n4; j0 += kHistVec * kThreads) {
+        float4 q[kHistVec];
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) q[u] = __ldg(k4 + j0 + u * kThreads + ti);
+        uint32_t miss = 0;
+#pragma unroll
+        for (int u = 0; u < kHistVec; ++u) {
+            const float kk[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (kk[c] < L) ++below;
+                if (kk[c] >= L && kk[c] < R) miss |= 1u << (4 * u + c);
+            }
+        }
+        while (miss) {
+            const uint32_t b = (uint32_t)__ffs(miss) - 1u;
+            miss &= miss - 1u;
+            key(__ldg(kb + 4 * (j0 + (b >> 2) * kThreads + ti) + (b & 3u)));
+        }
+    }
+    for (uint32_t j = j0 + ti; j < n4; j += kThreads) {
+        const float4 q = __ldg(k4 + j);
+        one(q.x);
+        one(q.y);
+        one(q.z);
+        one(q.w);
+    }
+    for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += kThreads) one(__ldg(keys + i));
+}
+
 // Whether pass v.pass over cell c (`tiles` tiles) is sparse: only the bracket's keys are
 // binned, the keys below it counted. The first pass of a cold level is dense for every cell;
 // later passes are sparse once the bracket holds at most sparse_per_tile keys a tile.
 __device__ __forceinline__ bool sparse_pass(const Level &v, int c, uint32_t tiles) {
     return !(v.pass == 0 && v.warm == nullptr) && v.inb[c] <= v.sparse_per_tile * tiles;
+}
+
+// ------------------------------------------------------------------------------------
+// Sampled first pass. The first count pass of a cold level bins every key of a cell into
+// the 2^K leaves of its midpoint tree. k_sample_bin and k_sample_pick predict from a strided
+// sample of the cell
+// (one key per 2^kSampleShift) a run of leaves [lo, hi) holding the cut: the sample's
+// median +- pred_sigmas standard errors (sqrt(s)/2 sample keys), widened to leaf edges
+// a = e(lo), b = e(hi). That pass then counts the keys below a and bins only the keys of
+// [a, b). Its replay in k_resolve is the reference loop unchanged once the exact counts
+// show count(< a) with difference <= -3 and count(< b) with difference >= 3: every tested
+// cut below a then has a count <= count(< a) and moves L, every cut above b has one
+// >= count(< b) and moves R (the float test is monotone in the count), and cuts inside
+// [a, b] get their exact counts from the bins. Otherwise the pass is discarded and the
+// next one bins every key. Same cuts, same integer counts, same iterations either way.
+// (k_resolve checks the counts; sample sizes and widths only change the speed.)
+// ------------------------------------------------------------------------------------
+constexpr uint32_t kPredValid = 1u << 25, kPredCompact = 1u << 24;
+__device__ __forceinline__ uint32_t pred_lo(uint32_t p) { return p & 0xfffu; }
+__device__ __forceinline__ uint32_t pred_hi(uint32_t p) { return (p >> 12) & 0xfffu; }
+constexpr int kSampleThreads = 256;
+constexpr int kSampleShift = 8;              // one sample key per 256 keys of the cell
+constexpr uint32_t kSampleMax = 16384;       // sample keys per cell at most
+constexpr uint32_t kSampleMin = 1024;        // fewer: no prediction (a dense first pass)
+constexpr uint32_t kSamplePerCta = 4 * kSampleThreads;
+constexpr float kPredCompactShare = 0.09f;   // compact the bracket keys when the sample puts
+                                             // at most this share of the cell inside it
+static_assert(kPredCompactShare * kTile * 1.25f < kCmpTile, "a tile's bracket keys fit the buffer");
+
+__device__ __forceinline__ uint32_t sample_count(uint32_t n) {
+    const uint32_t ns = min(n >> kSampleShift, kSampleMax);
+    return ns >= kSampleMin ? ns : 0u;
+}
+
+// Sample binning: CTA (x, y) takes samples [x kSamplePerCta, (x+1) kSamplePerCta) of the
+// cells y, y + gridDim.y, ...; sample j of a cell of n keys is the key at position
+// ((2j+1) n / (2 ns)) (fixed point), binned into the cell's histogram bins (all zero
+// between passes) by the scaled guess or the descent; samples below L are counted in
+// pred[c], which k_sample_pick then replaces by the prediction.
+__global__ void __launch_bounds__(kSampleThreads) k_sample_bin(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    const uint32_t ti = threadIdx.x;
+    for (int c = blockIdx.y; c < v.C; c += gridDim.y) {
+        if (v.state[c] != kActive) continue;
+        const int slot = level_slot(v, c);
+        const uint2 rg = v.ranges[slot];
+        const uint32_t n = rg.y - rg.x;
+        const uint32_t ns = sample_count(n);
+        const uint32_t j0 = blockIdx.x * kSamplePerCta;
+        if (j0 >= ns) continue;
+        const orb_cell_t &cell = v.heap[slot];
+        const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+        const int K = v.hist_k[c];
+        const uint32_t nb = 1u << K;
+        const float *keys = axis_keys(v, eff_axis(cell.cutAxis)) + rg.x;
+        uint32_t *gh = v.hist + v.hist_off[c];
+        // (2j+1) step >> 17 < n for j < ns: step = floor(n 2^16 / ns) < 2^37, products < 2^52
+        const uint64_t step = ((uint64_t)n << 16) / ns;
+        float k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = j0 + u * kSampleThreads + ti;
+            k[u] = j < ns ? __ldg(keys + (uint32_t)(((2ull * j + 1ull) * step) >> 17)) : R;
+        }
+        const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
+        const Guess gs = make_guess(L, R, scale, nb);
+        uint32_t below = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k[u] < L) {
+                ++below;
+            } else if (k[u] < R) {
+                uint32_t g;
+                if (!guess_bin(gs, k[u], &g)) g = (uint32_t)tree_bin(k[u], L, R, K);
+                atomicAdd(&gh[g], 1u);
+            }
+        }
+        below = warp_sum(below);
+        if ((ti & 31u) == 0 && below) atomicAdd(&v.pred[c], below);
+        if (ti == 0) add_bytes(v, kKSample, 4ull * min(kSamplePerCta, ns - j0));
+    }
+}
+
+// One CTA per sampled cell (cells y, y + gridDim.x, ...): the leaves [lo, hi) around the
+// sample median (+- pred_sigmas standard errors), packed into pred[c]; the bins are cleared
+// again. Each thread holds 8 consecutive bins in registers.
+constexpr int kPickThreads = 256;
+static_assert((1 << kMaxBinsLog2) == 8 * kPickThreads, "8 bins a thread");
+__global__ void __launch_bounds__(kPickThreads) k_sample_pick(Level v) {
+    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    __shared__ uint32_t s_red[72];
+    const uint32_t ti = threadIdx.x;
+    for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
+        if (v.state[c] != kActive) continue;
+        const uint2 rg = v.ranges[level_slot(v, c)];
+        const uint32_t ns = sample_count(rg.y - rg.x);
+        if (!ns) continue;
+        const uint32_t nb = 1u << v.hist_k[c];
+        uint4 *gh4 = reinterpret_cast<uint4 *>(v.hist + v.hist_off[c]);
+        const uint32_t below = v.pred[c];  // samples below L
+        // thread t owns leaves [8t, 8t + 8) (none past nb)
+        uint32_t h[8];
+        if (8 * ti < nb) {
+            const uint4 a = gh4[2 * ti], b = gh4[2 * ti + 1];
+            h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+            h[4] = b.x; h[5] = b.y; h[6] = b.z; h[7] = b.w;
+            gh4[2 * ti] = make_uint4(0u, 0u, 0u, 0u);
+            gh4[2 * ti + 1] = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) h[i] = 0u;
+        }
+        uint32_t run = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) run += h[i];
+        uint32_t total, unused;
+        const uint32_t pre = block_excl_scan2(run, 0u, s_red, &total, &unused).x;
+        const float half = 0.5f * (float)ns, w = v.pred_sigmas * 0.5f * sqrtf((float)ns);
+        const float r_lo = half - w, r_hi = half + w;
+        // cum(j) = samples below edge e(j) = below + bins [0, j); count the edges j in [0, nb]
+        // with cum(j) <= r_lo and with cum(j) < r_hi
+        uint32_t n_le = 0, n_lt = 0, cum = below + pre;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const bool own = 8 * ti + i < nb;
+            n_le += own && (float)cum <= r_lo;
+            n_lt += own && (float)cum < r_hi;
+            cum += h[i];
+        }
+        if (ti == 0) {
+            n_le += (float)(below + total) <= r_lo;
+            n_lt += (float)(below + total) < r_hi;
+        }
+        n_le = block_sum(n_le, s_red);
+        n_lt = block_sum(n_lt, s_red);
+        // lo: the last edge with at most r_lo samples below it; hi: the first with at least r_hi
+        const uint32_t lo = n_le ? n_le - 1u : 0u, hi = min(n_lt, nb);
+        uint32_t ca = 0, cb = 0;
+        cum = below + pre;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (8 * ti + i == lo) ca = cum;
+            if (8 * ti + i == hi) cb = cum;
+            cum += h[i];
+        }
+        ca = block_sum(ca, s_red);
+        cb = hi == nb ? below + total : block_sum(cb, s_red);
+        if (ti == 0) {
+            uint32_t p = 0u;
+            if (n_le > 0 && lo < hi && (lo > 0 || hi < nb)) {
+                const float share = (float)(cb - ca) / (float)ns;
+                p = lo | (hi << 12) | kPredValid | (share <= kPredCompactShare ? kPredCompact : 0u);
+                atomicAdd(&v.counters->pred_cells, 1u);
+            }
+            v.pred[c] = p;
+        }
+        __syncthreads();  // s_red reused by the next cell
+    }
 }
 
 // One count-left pass over the tiles of the level's active cells (cells of more than one
@@ -747,11 +1087,22 @@ __device__ __forceinline__ bool sparse_pass(const Level &v, int c, uint32_t tile
 // consecutive tiles (runs of equal length to one tile); a cell's shared bins, count below
 // and compacted keys stay with the CTA while its tiles follow one another and are added to
 // the global ones once per run.
+// Allowed: the modes this instance handles (the other paths are compiled out, which keeps
+// each instance's streaming loop within its registers): kHFirstDense, the first pass of a
+// cold level without sampled brackets (every cell dense); kHFirstSampled, the first pass of
+// a sampled level (sampled or dense cells); kHRest, every other pass.
+constexpr uint32_t kHSparse = 32;  // (allowed only) the sparse modes
+constexpr uint32_t kHFirstDense = kHDense;
+constexpr uint32_t kHFirstSampled = kHDense | kHPred | kHCompact;
+constexpr uint32_t kHRest = kHDense | kHLocal | kHCompact | kHListed | kHSparse;
+template <uint32_t Allowed>
 __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    constexpr bool kAny = Allowed != kHDense;
     __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
+    __shared__ float s_edge[(1 << kMaxBinsLog2) + 1];      // dense and sampled: the tree's edges
     __shared__ uint32_t s_red[32];
-    __shared__ float s_cmp[kCmpTile];  // a sparse tile's bracket keys, on their way to the list
+    __shared__ float s_cmp[(Allowed & kHCompact) ? kCmpTile : 1];  // bracket keys on their way to the list
     __shared__ uint32_t s_ncmp, s_base;
     __shared__ HistCell s_hc;
     __shared__ uint32_t s_run[2];           // the CTA's tiles [first, end)
@@ -777,7 +1128,7 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
             const uint32_t tot = below + s_hc.below;
             if (tot) atomicAdd(&v.below[cur], tot);
         }
-        if (mode & (kHDense | kHLocal)) {
+        if (mode & (kHDense | kHLocal | kHPred)) {
             const uint32_t nb = 1u << s_hc.K;
             uint32_t *gh = s_hc.gh;
             for (uint32_t b = threadIdx.x; b < nb; b += kThreads) {
@@ -785,17 +1136,28 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
                 if (h) atomicAdd(&gh[b], h);
             }
         }
-        if (mode & kHCompact) {
+        if ((Allowed & kHCompact) && (mode & kHCompact)) {
             const uint32_t wrote = append_list(v, cur, s_cmp, &s_ncmp, &s_base);
             if (threadIdx.x == 0) s_bytes += 4ull * wrote;
         }
         __syncthreads();  // s_hc and s_hist free for the next cell
         below = 0;
     };
-    for (uint32_t t = s_run[0]; t < s_run[1]; ++t) {
-        const int c = v.htile_cell ? (int)v.htile_cell[t] : find_cell(v.tile_off, v.C, t);
-        if (v.state[c] != kActive) continue;
+    const uint32_t t_end = s_run[1];
+    auto tile_cell = [&](uint32_t t) {
+        return t < t_end ? (v.htile_cell ? (int)v.htile_cell[t] : find_cell(v.tile_off, v.C, t)) : -1;
+    };
+    int c_next = tile_cell(s_run[0]);
+    int skip_c = -1;  // an inactive cell whose tiles are being passed over
+    for (uint32_t t = s_run[0]; t < t_end; ++t) {
+        const int c = c_next;
+        c_next = tile_cell(t + 1);  // the next tile's cell, loaded while this tile is read
+        if (c == skip_c) continue;
         if (c != cur) {
+            if (v.state[c] != kActive) {  // the run's tiles of a cell are consecutive
+                skip_c = c;
+                continue;
+            }
             if (cur >= 0) end_cell();
             cur = c;
             if (threadIdx.x == 0) {
@@ -808,8 +1170,13 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
                 const uint32_t nb = 1u << K;
                 const float scale = __fdiv_rn((float)nb, __fsub_rn(R, L));
                 uint32_t mode;
-                if (v.listed[c])
+                const uint32_t pr = (Allowed & kHPred) && v.pass == 0 && v.pred ? v.pred[c] : 0u;
+                if (!kAny)
+                    mode = kHDense;  // a cold first pass without sampled brackets
+                else if ((Allowed & kHListed) && v.listed[c])
                     mode = kHListed;
+                else if (pr & kPredValid)
+                    mode = kHPred | (pr & kPredCompact ? kHCompact : 0u);
                 else if (!sparse_pass(v, c, tiles))
                     mode = kHDense;
                 else
@@ -828,17 +1195,21 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
                 s_hc.end = rg.y;
                 s_hc.t0 = t0;
                 s_hc.below = 0;
+                s_hc.pa = pr & kPredValid ? tree_edge(L, R, K, pred_lo(pr)) : L;
+                s_hc.pb = pr & kPredValid ? tree_edge(L, R, K, pred_hi(pr)) : R;
                 s_hc.gs = make_guess(L, R, scale, nb);
             }
             __syncthreads();
-            if (s_hc.mode & (kHDense | kHLocal)) {
+            if (s_hc.mode & (kHDense | kHLocal | kHPred)) {
                 for (uint32_t j = threadIdx.x; j < (1u << s_hc.K); j += kThreads) s_hist[j] = 0u;
+                if (s_hc.mode & (kHDense | kHPred))
+                    fill_edges(s_edge, s_hc.L, s_hc.R, s_hc.K, threadIdx.x, kThreads);
                 __syncthreads();
             }
         }
         const uint32_t local = t - s_hc.t0;
         const uint32_t mode = s_hc.mode;
-        if (mode & kHListed) {
+        if ((Allowed & kHListed) && (mode & kHListed)) {
             const uint32_t nread = listed_tile(v, c, local, &s_hc);
             if (threadIdx.x == 0) s_bytes += 4ull * nread;
             continue;
@@ -846,39 +1217,37 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
         const uint32_t e0 = s_hc.base + local * (uint32_t)kTile;
         const uint32_t e1 = min(s_hc.end, e0 + (uint32_t)kTile);
         const float *keys = s_hc.keys;
-        if (mode & kHDense) {
-            // the scaled guess alone, no range test (guess_bin fails keys outside [L, R)
-            // and NaN); a key it does not settle is counted in the lane's spare bin past the
-            // top (never read) and binned exactly afterwards
-            const Guess gs = s_hc.gs;
-            const uint32_t spare = (gs.lim >> 12) + (threadIdx.x & 31);
-            auto exact = [&](float k) { dense_exact(k, &s_hc, s_hist); };
-            scan_tile<kThreads>(
+        if ((Allowed & kHPred) && (mode & kHPred)) {
+            // sampled bracket [pa, pb): keys below it counted, keys inside it (a few percent)
+            // binned afterwards (and compacted, the list flushed after every tile so the
+            // buffer holds one tile's keys), keys above it and NaN ignored
+            const float pa = s_hc.pa, pb = s_hc.pb;
+            auto key = [&](float k) { pred_key(k, &s_hc, s_hist, s_cmp, &s_ncmp, s_edge); };
+            scan_tile<kThreads, true>(
                 keys, e0, e1, s_hc.R,
                 [&](float k) {
-                    uint32_t g;
-                    const bool ok = guess_bin(gs, k, &g);
-                    atomicAdd(&s_hist[ok ? g : spare], 1u);
-                    return ok;
-                },
-                exact, exact);
-        } else {
-            // keys below L counted, keys in [L, R) (few) binned afterwards
-            const float L = s_hc.L, R = s_hc.R;
-            auto key = [&](float k) { sparse_key(k, &s_hc, s_hist, s_cmp, &s_ncmp); };
-            scan_tile<kThreads>(
-                keys, e0, e1, R,
-                [&](float k) {
-                    below += k < L;
-                    return !(k >= L && k < R);
+                    below += k < pa;
+                    return !(k >= pa && k < pb);
                 },
                 key,
                 [&](float k) {
-                    if (k < L)
+                    if (k < pa)
                         ++below;
-                    else if (k < R)
+                    else if (k < pb)
                         key(k);
                 });
+            if (mode & kHCompact) {
+                const uint32_t wrote = append_list(v, c, s_cmp, &s_ncmp, &s_base);
+                if (threadIdx.x == 0) s_bytes += 4ull * wrote;
+            }
+        } else if (!kAny || (mode & kHDense)) {
+            // every key by the scaled guess (no range test: guess_bin fails keys outside
+            // [L, R) and NaN, which dense_exact then counts or ignores)
+            dense_tile(keys, e0, e1, s_hc.gs, s_hist, &s_hc, s_edge);
+        } else if (Allowed & kHSparse) {
+            // keys below L counted, keys in [L, R) (few) binned after their round
+            sparse_tile(keys, e0, e1, s_hc.L, s_hc.R, below,
+                        [&](float k) { sparse_key(k, &s_hc, s_hist, s_cmp, &s_ncmp); });
         }
         if (threadIdx.x == 0) s_bytes += 4ull * (e1 - e0);
     }
@@ -1107,6 +1476,28 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         return warp_sum((b0 >= a && b0 < a + w ? pair.x : 0u) + (b0 + 1 >= a && b0 + 1 < a + w ? pair.y : 0u));
     };
     uint32_t first_half = 0xffffffffu;  // bins below the first cut, when already summed
+    const uint32_t pr = v.pass == 0 && v.pred ? v.pred[c] : 0u;
+    if (pr & kPredValid) {
+        // sampled pass: prefix = keys below e(lo), the bins hold the keys of [e(lo), e(hi));
+        // the replay below is exact when the cut lies between them (see k_sample_bin)
+        const uint32_t tot = sum_bins(0, 1u << K);
+        const bool holds = convergence(prefix, n) < 0 && convergence(prefix + tot, n) > 0;
+        __syncwarp();
+        if (!holds) {
+            for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
+            if (lane == 0) {
+                v.inb[c] = n;  // the next pass bins every key (dense)
+                v.below[c] = 0;
+                v.listed[c] = 0;
+                v.cmp_cnt[c] = 0;
+                v.cmp_bad[c] = 0;
+                v.counters->any_active[v.pass & 1] = 1u;
+                atomicAdd(&v.counters->pred_misses, 1u);
+                add_bytes(v, kKResolve, 8ull << K);
+            }
+            return;
+        }
+    }
     if (v.warm && v.warm[c]) {
         // first pass of a hinted bracket: check it holds the target before replaying (the
         // total and the first step's count)
@@ -1160,8 +1551,9 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     // the next pass reads the cell's list when this pass read one or wrote a complete one
     // (a sparse pass compacts its bracket keys); then the keys below the new L are known
     const uint32_t tiles = v.tile_off[c + 1] - v.tile_off[c];
-    const bool list_next = v.listed[c] || (sparse_pass(v, c, tiles) &&
-                                           v.inb[c] > (8u << K) && !v.cmp_bad[c]);
+    const bool compacted = pr & kPredValid ? (pr & kPredCompact) != 0
+                                           : sparse_pass(v, c, tiles) && v.inb[c] > (8u << K);
+    const bool list_next = v.listed[c] || (compacted && !v.cmp_bad[c]);
     __syncwarp();
     for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
     if (st == kActive && lane == 0) {
@@ -1448,6 +1840,7 @@ __global__ void k_tile_map(Level v) {
             v.cmp_cnt[t] = 0;
             v.listed[t] = 0;
             v.cmp_bad[t] = 0;
+            if (v.pred) v.pred[t] = 0u;  // no sampled bracket unless k_sample_pick sets one
         }
     }
 }
@@ -2533,8 +2926,13 @@ void launch_init(const Level &v, uint64_t n, const float lower[3], const float u
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st) {
     switch (k) {
         case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
-        case kKHist:
-            k_hist<<<grid, kThreads, 0, st>>>(v);
+        case kKHist:  // arg: 1 first pass, all cells dense; 2 first pass of a sampled level
+            if (arg == 1)
+                k_hist<kHFirstDense><<<grid, kThreads, 0, st>>>(v);
+            else if (arg == 2)
+                k_hist<kHFirstSampled><<<grid, kThreads, 0, st>>>(v);
+            else
+                k_hist<kHRest><<<grid, kThreads, 0, st>>>(v);
             break;
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
@@ -2560,6 +2958,10 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
             k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, arg);
             break;
         case kKCountLeft: k_count_left<<<grid, kThreads, 0, st>>>(v); break;
+        case kKSample:
+            k_sample_bin<<<dim3(kSampleMax / kSamplePerCta, (unsigned)min(v.C, 65535)), kSampleThreads, 0, st>>>(v);
+            break;
+        case kKSamplePick: k_sample_pick<<<min(v.C, 65535), kPickThreads, 0, st>>>(v); break;
         default: break;
     }
 }

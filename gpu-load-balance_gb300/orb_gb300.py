@@ -25,7 +25,8 @@ HEADERS = ["orb_internal.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
-              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills",
+              *os.environ.get("ORB_NVCC_FLAGS", "").split()]  # extra flags (build-time knobs)
 
 CELL_DTYPE = np.dtype(
     [
@@ -131,6 +132,7 @@ class Tuning(ctypes.Structure):
         ("sparse_keys_per_tile", ctypes.c_uint32),
         ("cta_min_cells", ctypes.c_uint32),
         ("subtree_levels", ctypes.c_uint32),
+        ("predict_sigmas", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -150,6 +152,8 @@ class BuildInfo(ctypes.Structure):
         ("d2h_ms", ctypes.c_float),
         ("warm_cells", ctypes.c_uint32),
         ("warm_resets", ctypes.c_uint32),
+        ("sampled_cells", ctypes.c_uint32),
+        ("sampled_misses", ctypes.c_uint32),
     ]
 
     def as_dict(self):

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define ORB_ABI_VERSION 2
+#define ORB_ABI_VERSION 3
 
 typedef enum orb_status {
     ORB_OK = 0,
@@ -89,6 +89,10 @@ typedef struct orb_build_info {
     float d2h_ms;               /* device->host copy time (host-pointer calls) */
     uint32_t warm_cells;        /* warm builds: cells that started from a hinted bracket */
     uint32_t warm_resets;       /* ... whose hinted bracket missed the target and restarted */
+    uint32_t sampled_cells;     /* cells whose first count pass used a bracket predicted from a
+                                   sample of their keys (result-invariant, see orb_tuning) */
+    uint32_t sampled_misses;    /* ... whose predicted bracket did not hold the cut (that pass
+                                   was repeated over every key) */
 } orb_build_info;
 
 /* Context lifetime. device = CUDA ordinal. opts may be NULL. */
@@ -188,6 +192,12 @@ typedef struct orb_tuning {
     uint32_t subtree_levels;       /* the last levels (at most this many, 0..6, default 3) are
                                       finished by one CTA per cell once every cell of a level
                                       fits one (at most 17408 particles); 0 = never */
+    uint32_t predict_sigmas;       /* first count pass of cells of at least 2^18 particles: the
+                                      keys are binned only inside a bracket predicted from a
+                                      strided sample (its median +- this many standard errors),
+                                      checked exactly, repeated over every key when it misses;
+                                      0..16, 0 = never (default 0: slower on the measured
+                                      workloads; the autotuner tries it) */
 } orb_tuning;
 
 orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out);

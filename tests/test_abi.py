@@ -35,7 +35,7 @@ def test_library_is_sm103a(engine):
 
 def test_status_strings(engine):
     lib = engine.load()
-    assert lib.orb_abi_version() == 2
+    assert lib.orb_abi_version() == 3
     for code, text in engine.STATUS.items():
         assert lib.orb_status_string(code).decode() == text
 
@@ -50,8 +50,8 @@ def test_cell_layout(engine):
 
 
 def test_tuning_layout_and_null_checks(engine):
-    # orb_tuning: six uint32 fields, no padding
-    assert ctypes.sizeof(engine.Tuning) == 24
+    # orb_tuning: seven uint32 fields, no padding
+    assert ctypes.sizeof(engine.Tuning) == 28
     lib = engine.load()
     t = engine.Tuning()
     assert lib.orb_get_tuning(None, ctypes.byref(t)) == 1

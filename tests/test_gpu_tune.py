@@ -10,11 +10,11 @@ pytestmark = pytest.mark.gpu
 
 EXTREMES = [
     dict(hist_blocks_per_sm=1, part_blocks_per_sm=1, tile_blocks_per_sm=1, sparse_keys_per_tile=1,
-         cta_min_cells=0, subtree_levels=0),
+         cta_min_cells=0, subtree_levels=0, predict_sigmas=0),
     dict(hist_blocks_per_sm=8, part_blocks_per_sm=16, tile_blocks_per_sm=4,
-         sparse_keys_per_tile=16384, cta_min_cells=0, subtree_levels=6),
+         sparse_keys_per_tile=16384, cta_min_cells=0, subtree_levels=6, predict_sigmas=16),
     dict(hist_blocks_per_sm=3, part_blocks_per_sm=5, tile_blocks_per_sm=2, sparse_keys_per_tile=7,
-         cta_min_cells=64, subtree_levels=2),
+         cta_min_cells=64, subtree_levels=2, predict_sigmas=1),
 ]
 
 
@@ -27,14 +27,15 @@ def fresh(engine):
 
 def test_get_set_roundtrip_and_limits(fresh, engine):
     d = fresh.get_tuning()
-    assert d == dict(hist_blocks_per_sm=8, part_blocks_per_sm=8, tile_blocks_per_sm=4,
-                     sparse_keys_per_tile=64, cta_min_cells=0, subtree_levels=3)
+    assert d == dict(hist_blocks_per_sm=6, part_blocks_per_sm=8, tile_blocks_per_sm=4,
+                     sparse_keys_per_tile=64, cta_min_cells=0, subtree_levels=3, predict_sigmas=0)
     fresh.set_tuning(part_blocks_per_sm=12, sparse_keys_per_tile=100)
     assert fresh.get_tuning()["part_blocks_per_sm"] == 12
     assert fresh.get_tuning()["sparse_keys_per_tile"] == 100
     for bad in (dict(hist_blocks_per_sm=0), dict(hist_blocks_per_sm=9), dict(part_blocks_per_sm=17),
                 dict(tile_blocks_per_sm=9), dict(sparse_keys_per_tile=0),
-                dict(sparse_keys_per_tile=16385), dict(subtree_levels=7)):
+                dict(sparse_keys_per_tile=16385), dict(subtree_levels=7),
+                dict(predict_sigmas=17)):
         with pytest.raises(engine.OrbError):
             fresh.set_tuning(**bad)
     assert fresh.get_tuning()["part_blocks_per_sm"] == 12  # a refused setting changes nothing
