@@ -153,6 +153,20 @@ bool is_device_ptr(const void *p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// The device-accessible address of pinned (page-locked or registered) host memory; false for
+// any other pointer.
+template <class T>
+bool host_device_ptr(T *p, T **out) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+    *out = static_cast<T *>(a.devicePointer);
+    return true;
+}
+
 orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
     ORB_CUDA(ctx->ptile_cell.ensure(ptiles));
     ORB_CUDA(ctx->ge_bits.ensure(ptiles * kPWords));
@@ -688,6 +702,14 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     const int sub_from = subtree_from(ctx, lv, n, levels == (uint32_t)ylev);
     if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
     key.push_back((uint64_t)(int64_t)sub_from);
+    // pinned host outputs of a build that plans subtrees: the subtree kernel writes every
+    // finished cell straight into them (the transfer overlaps the last levels)
+    const bool direct = !dev && n && sub_from >= 0 && host_device_ptr(x, &v.hx) &&
+                        host_device_ptr(y, &v.hy) && host_device_ptr(z, &v.hz) &&
+                        (!perm || host_device_ptr(perm, &v.hperm));
+    if (!direct) v.hx = v.hy = v.hz = nullptr, v.hperm = nullptr;
+    for (const void *p : {(const void *)v.hx, (const void *)v.hy, (const void *)v.hz, (const void *)v.hperm})
+        key_add(key, p);
     uint32_t passes = 0;
     st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
         ctx->launches[kKInit] += 1;
@@ -697,17 +719,23 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    bool written = false;  // the subtree kernel wrote the particles to the host arrays
     if (!dev) {
         ORB_CUDA(cudaStreamSynchronize(s));
         ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
+        if (direct) {
+            uint32_t taken = 0;
+            ORB_CUDA(cudaMemcpy(&taken, ctx->sub_flag.p, sizeof taken, cudaMemcpyDeviceToHost));
+            written = taken != 0;
+        }
         ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
-        if (n) {
+        if (n && !written) {
             ORB_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(float), cudaMemcpyDeviceToHost, s));
             ORB_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, s));
             ORB_CUDA(cudaMemcpyAsync(z, dz, n * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
     }
-    if (perm && n)
+    if (perm && n && !written)
         ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n * sizeof(uint32_t),
                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     ORB_CUDA(cudaMemcpyAsync(heap, ctx->heap.p, heap_cells * sizeof(orb_cell_t), cudaMemcpyDeviceToHost, s));

@@ -134,6 +134,11 @@ struct Level {
     // subtrees: 1 when one CTA per cell finishes the tree from this level down (then the
     // level kernels of the levels below return at once); null when not attempted
     uint32_t *skip;
+    // single builds from pinned host arrays (null otherwise): device-accessible addresses of
+    // the caller's x, y, z (and permutation) arrays; the subtree kernel writes each finished
+    // cell's final particles there, overlapping the device-to-host transfer with the last levels
+    float *hx, *hy, *hz;
+    uint32_t *hperm;
     BuildCounters *counters;
 };
 

@@ -2723,6 +2723,27 @@ __global__ void __launch_bounds__(1024) k_subtree_check(Level v, int max_levels)
 
 // One CTA per cell of the level: every level below it (its leaf count's log2), breadth
 // first.
+// dst[i] = src[i] for i in [b, e) by the CTA (dst: host memory reached over the C2C link):
+// 16-byte stores when both arrays have the same alignment, else 4-byte ones.
+template <class T>
+__device__ void copy_out(const T *src, T *dst, uint32_t b, uint32_t e) {
+    static_assert(sizeof(T) == 4, "4-byte elements");
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(src + b), da = reinterpret_cast<uintptr_t>(dst + b);
+    uint32_t a0 = b;
+    if (((sa ^ da) & 15u) == 0) {
+        a0 = min(e, b + (uint32_t)(((16u - (sa & 15u)) & 15u) >> 2));
+        const uint32_t n4 = (e - a0) >> 2;
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src + a0);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst + a0);
+        for (uint32_t j = tid; j < n4; j += nt) d4[j] = s4[j];
+        for (uint32_t i = b + tid; i < a0; i += nt) dst[i] = src[i];
+        for (uint32_t i = a0 + (n4 << 2) + tid; i < e; i += nt) dst[i] = src[i];
+    } else {
+        for (uint32_t i = b + tid; i < e; i += nt) dst[i] = src[i];
+    }
+}
+
 __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
@@ -2749,6 +2770,13 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
             __syncthreads();
             cur ^= 1;
             nq = nn;
+        }
+        if (v.hx) {  // the cell's particles are final: to the caller's host arrays
+            const uint2 rg = v.ranges[root];
+            copy_out(v.x, v.hx, rg.x, rg.y);
+            copy_out(v.y, v.hy, rg.x, rg.y);
+            copy_out(v.z, v.hz, rg.x, rg.y);
+            if (v.hperm && v.idx) copy_out(v.idx, v.hperm, rg.x, rg.y);
         }
     }
     if (threadIdx.x == 0 && bytes) add_bytes(v, kKSubtree, bytes);
