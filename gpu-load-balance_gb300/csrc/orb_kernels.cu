@@ -2721,8 +2721,6 @@ __global__ void __launch_bounds__(1024) k_subtree_check(Level v, int max_levels)
         *v.skip = mx <= kSubMax && (int)ml <= min(max_levels, kSubLevels) ? 1u : 0u;
 }
 
-// One CTA per cell of the level: every level below it (its leaf count's log2), breadth
-// first.
 // dst[i] = src[i] for i in [b, e) by the CTA (dst: host memory reached over the C2C link):
 // 16-byte stores when both arrays have the same alignment, else 4-byte ones.
 template <class T>
@@ -2744,6 +2742,8 @@ __device__ void copy_out(const T *src, T *dst, uint32_t b, uint32_t e) {
     }
 }
 
+// One CTA per cell of the level: every level below it (its leaf count's log2), breadth
+// first; with host outputs (v.hx), the finished cell's particles are then written there.
 __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
