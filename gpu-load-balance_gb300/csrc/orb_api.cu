@@ -437,7 +437,10 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
 // first: the count pass the first pass uses: 1 every cell dense (a cold level without
 // sampled brackets), 2 a sampled level, 0 the general one (warm builds).
 orb_status run_bisection(orb_ctx *ctx, Level v, uint32_t *passes, int first) {
-    for (int pass = 0; pass < kHistPasses; ++pass) {
+    // a cold first pass over every key is never discarded: 3 passes reach the cap
+    const int npasses = first == 1 ? kColdHistPasses : kHistPasses;
+    v.last_pass = npasses - 1;
+    for (int pass = 0; pass < npasses; ++pass) {
         v.pass = pass;
         run_kernel(ctx, kKHist, v, ctx->num_sms * (int)ctx->tune.hist_blocks_per_sm,
                    pass == 0 ? first : 0);
@@ -507,7 +510,6 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
                 run_kernel(ctx, kKSample, v, 0);
                 run_kernel(ctx, kKSamplePick, v, 0);
             }
-            run_kernel(ctx, kKBisectWarp, v, 1);  // cells small enough for one warp
             run_kernel(ctx, kKBisectTile, v, std::min(v.C, ctx->num_sms * (int)ctx->tune.tile_blocks_per_sm));
             orb_status st = run_bisection(ctx, v, passes, v.hint ? 0 : (sampled ? 2 : 1));
             if (st != ORB_OK) return st;

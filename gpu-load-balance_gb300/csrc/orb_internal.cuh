@@ -16,9 +16,12 @@ constexpr int kTile = 16384;         // keys per tile of the count-left passes
 constexpr int kPTile = 4096;         // positions per tile of the partition passes
 constexpr int kPWords = kPTile / 32; // bitmask words per partition tile
 constexpr int kMaxBinsLog2 = 11;     // deepest midpoint tree one histogram pass resolves
-// Histogram passes per level. Cells of more than kWarpKeys keys use trees of depth >= 9
-// (tree_depth), so ceil(32 / 9) = 4 passes finish every bisection (at most 32 iterations).
+// Histogram passes per level. The count passes bisect cells of more than kTile keys, whose
+// trees have depth 11 (tree_depth), so 3 passes (33 iterations) reach the 32-iteration cap
+// of every cell. A first pass that is discarded (a warm or sampled bracket that missed the
+// cut) costs one more, hence 4 for levels that may have one.
 constexpr int kHistPasses = 4;
+constexpr int kColdHistPasses = 3;
 constexpr int kThreads = 256;
 // resident CTAs of the count-left pass (its launch bound: 65536 / (256 x 6) = 40 registers)
 #ifndef ORB_HIST_BLOCKS_PER_SM
@@ -49,7 +52,7 @@ enum Kernel : int {
     kKGenerate,
     kKBisectCta,
     kKTileMap,
-    kKBisectWarp,
+    kKBisectWarp,  // bytes of the small cells k_bisect_tile bisects in registers (no launch)
     kKBisectTile,
     kKWarmStart,
     kKSubtreeCheck,
@@ -88,6 +91,7 @@ struct Level {
     int base;
     int C;
     int pass;               // histogram pass index within the level
+    int last_pass;          // index of the level's last histogram pass
     // plan
     uint32_t *tile_off;     // [C+1] first tile of each cell
     uint32_t *htile_cell;   // [tiles] cell of each count-left tile (null: binary search)

@@ -207,6 +207,10 @@ __host__ __device__ __forceinline__ uint32_t list_capacity(uint32_t n) {
     return n > (uint32_t)kTile ? (n / 8 > 2048u ? n / 8 : 2048u) : 0u;
 }
 
+// Cells of more than kTile keys (the count passes' cells) get the deepest tree, so the cold
+// passes reach the iteration cap.
+static_assert(kTile >= (2 << kMaxBinsLog2), "cells of more than kTile keys get trees of depth 11");
+static_assert(kColdHistPasses * kMaxBinsLog2 >= kMaxIterations, "3 cold passes reach the cap");
 __device__ __forceinline__ int tree_depth(uint32_t n) {
     int lg = 31 - __clz(max(n, 1u));  // floor(log2 n)
     return max(4, min(kMaxBinsLog2, lg - 1));
@@ -1264,6 +1268,73 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
 // register count plus a warp sum. Every round streams the cell's keys (L2-resident after
 // the first).
 // ------------------------------------------------------------------------------------
+constexpr int kWarpKeysPerLane = kWarpKeys / 32;
+
+// Bisection of a small cell (at most kWarpKeys keys) by one warp: the keys held in registers,
+// every iteration of the reference loop (src/orbit.cpp:146-232) a register count plus a
+// warp reduction.
+__device__ __forceinline__ void bisect_small(const Level &v, int c, uint32_t lane) {
+    const int slot = level_slot(v, c);
+    orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    float k[kWarpKeysPerLane];
+#pragma unroll
+    for (int j = 0; j < kWarpKeysPerLane; ++j) {
+        const uint32_t i = (uint32_t)(j * 32 + lane);
+        k[j] = i < n ? __ldg(keys + rg.x + i) : __int_as_float(0x7fc00000);  // NaN: never below
+    }
+    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    if (v.warm && v.warm[c]) {
+        // hinted bracket: keep it only if it holds the target
+        uint32_t bl = 0, br = 0;
+#pragma unroll
+        for (int j = 0; j < kWarpKeysPerLane; ++j) {
+            bl += k[j] < L;
+            br += k[j] < R;
+        }
+        if (!warm_bracket_holds(warp_sum(bl), warp_sum(br), n)) {
+            const int a = eff_axis(cell.cutAxis);
+            L = cell.lower[a];
+            R = cell.upper[a];
+            if (lane == 0) atomicAdd(&v.counters->warm_resets, 1u);
+        }
+        if (lane == 0) v.warm[c] = 0;
+    }
+    uint32_t it = 0;
+    uint8_t st = kActive;
+    while (st == kActive) {
+        if (it >= (uint32_t)kMaxIterations) {
+            st = kCapped;
+            break;
+        }
+        const float cut = mid_cut(L, R);
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
+        cnt = warp_sum(cnt);
+        ++it;
+        const int dir = convergence(cnt, n);
+        if (dir == 0)
+            st = kFound;
+        else if (dir > 0)
+            R = cut;
+        else
+            L = cut;
+    }
+    if (lane == 0) {
+        cell.cutMarginLeft = L;
+        cell.cutMarginRight = R;
+        cell.foundCut = st == kFound ? 1 : 0;
+        v.iters[c] = (uint8_t)it;
+        v.state[c] = st;
+        atomicMax(&v.counters->max_iters, it);
+        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+        add_bytes(v, kKBisectWarp, 4ull * n);
+    }
+}
+
 constexpr int kTileBinsLog2 = 9;
 constexpr int kTileBins = 1 << kTileBinsLog2;
 constexpr int kListPerLane = 8;     // bracket keys a lane can hold
@@ -1279,7 +1350,12 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
     const int nwarps = (int)(gridDim.x * (blockDim.x >> 5));
     unsigned long long bytes = 0;
     for (int c = (int)(blockIdx.x * (blockDim.x >> 5) + warp); c < v.C; c += nwarps) {
-        if (v.state[c] != kOneTile) continue;
+        const uint8_t state = v.state[c];
+        if (state == kSmall) {
+            bisect_small(v, c, lane);
+            continue;
+        }
+        if (state != kOneTile) continue;
         const int slot = level_slot(v, c);
         orb_cell_t &cell = v.heap[slot];
         const uint2 rg = v.ranges[slot];
@@ -1572,84 +1648,13 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
         if (st == kActive) {
             v.counters->any_active[v.pass & 1] = 1u;
-            // the last pass leaves no cell active (tree depths >= 9): flag it if one does
-            if (v.pass == kHistPasses - 1) atomicExch(&v.counters->error, 1u);
+            // the last pass leaves no cell active (tree depth 11): flag it if one does
+            if (v.pass == v.last_pass) atomicExch(&v.counters->error, 1u);
         }
     }
 }
 
-// ------------------------------------------------------------------------------------
-// Bisection of small cells (at most kWarpKeys keys): one warp per cell, the keys held in
-// registers, every iteration of the reference loop (src/orbit.cpp:146-232) a register
-// count plus a warp reduction. Cells of other sizes are left to the histogram passes.
-// ------------------------------------------------------------------------------------
-constexpr int kWarpKeysPerLane = kWarpKeys / 32;
 
-__global__ void __launch_bounds__(kThreads) k_bisect_warp(Level v) {
-    if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
-    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (c >= v.C || v.state[c] != kSmall) return;
-    const int slot = level_slot(v, c);
-    orb_cell_t &cell = v.heap[slot];
-    const uint2 rg = v.ranges[slot];
-    const uint32_t n = rg.y - rg.x;
-    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
-    float k[kWarpKeysPerLane];
-#pragma unroll
-    for (int j = 0; j < kWarpKeysPerLane; ++j) {
-        const uint32_t i = (uint32_t)(j * 32 + lane);
-        k[j] = i < n ? __ldg(keys + rg.x + i) : __int_as_float(0x7fc00000);  // NaN: never below
-    }
-    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
-    if (v.warm && v.warm[c]) {
-        // hinted bracket: keep it only if it holds the target
-        uint32_t bl = 0, br = 0;
-#pragma unroll
-        for (int j = 0; j < kWarpKeysPerLane; ++j) {
-            bl += k[j] < L;
-            br += k[j] < R;
-        }
-        if (!warm_bracket_holds(warp_sum(bl), warp_sum(br), n)) {
-            const int a = eff_axis(cell.cutAxis);
-            L = cell.lower[a];
-            R = cell.upper[a];
-            if (lane == 0) atomicAdd(&v.counters->warm_resets, 1u);
-        }
-        if (lane == 0) v.warm[c] = 0;
-    }
-    uint32_t it = 0;
-    uint8_t st = kActive;
-    while (st == kActive) {
-        if (it >= (uint32_t)kMaxIterations) {
-            st = kCapped;
-            break;
-        }
-        const float cut = mid_cut(L, R);
-        uint32_t cnt = 0;
-#pragma unroll
-        for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
-        cnt = warp_sum(cnt);
-        ++it;
-        const int dir = convergence(cnt, n);
-        if (dir == 0)
-            st = kFound;
-        else if (dir > 0)
-            R = cut;
-        else
-            L = cut;
-    }
-    if (lane == 0) {
-        cell.cutMarginLeft = L;
-        cell.cutMarginRight = R;
-        cell.foundCut = st == kFound ? 1 : 0;
-        v.iters[c] = (uint8_t)it;
-        v.state[c] = st;
-        atomicMax(&v.counters->max_iters, it);
-        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
-        add_bytes(v, kKBisectWarp, 4ull * n);
-    }
-}
 
 // ------------------------------------------------------------------------------------
 // Bisection with one CTA per cell, for levels with many cells (no multi-CTA passes, no
@@ -2970,9 +2975,6 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;
         case kKTileMap: k_tile_map<<<grid, kThreads, 0, st>>>(v); break;
-        case kKBisectWarp:
-            k_bisect_warp<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-            break;
         case kKResolve:
             k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
