@@ -1178,8 +1178,9 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
             key_add_f(key, inst[i].upper[a]);
         }
     }
-    // subtrees when every instance is built to its leaves (warm builds keep the level path)
-    bool full = !warm;
+    // subtrees when every instance is built to its leaves; in warm builds the subtree levels
+    // bisect from each cell's extent (hints apply to the levels above them)
+    bool full = true;
     uint64_t max_n = 0;
     for (uint32_t i = 0; i < k; ++i) {
         full = full && lev[i] == (uint32_t)log2_exact(inst[i].d);
