@@ -73,7 +73,7 @@ struct orb_ctx {
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint32_t> htile_cell, ptile_cell;
     // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
-    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 3u, 0u};
+    orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 4u, 0u};
     DevBuf<uint8_t> hist_k, state, iters, listed, cmp_bad;
     DevBuf<uint32_t> cmp_off, cmp_cnt, pred;
     DevBuf<float> cmp_keys;
@@ -482,19 +482,24 @@ int subtree_from(const orb_ctx *ctx, const std::vector<LevelDesc> &lv, uint64_t 
 // those levels then return at once.
 // max_n: the largest instance's particles (cells of level l hold about max_n >> l); levels
 // whose cells can be large enough get a sampled first count pass (k_sample_bin, k_sample_pick).
+// rest = false: the levels above sub_from, then (sub_from >= 0) the subtree check and the
+// subtree kernel for the levels from sub_from down; rest = true: the levels from sub_from
+// down one by one, for builds whose subtree path the device refused.
 orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes,
-                      int sub_from, uint64_t max_n) {
-    for (size_t li = 0; li < lv.size(); ++li) {
+                      int sub_from, uint64_t max_n, bool rest = false) {
+    for (size_t li = rest ? (size_t)sub_from : 0; li < lv.size(); ++li) {
         const LevelDesc &d = lv[li];
         v.base = d.base;
         v.slots = d.slots;
         v.C = d.C;
-        if (v.C == 0) continue;
-        if ((int)li == sub_from) {
+        if (!rest && (int)li == sub_from) {
+            if (v.C == 0) break;
             v.skip = ctx->sub_flag.p;
             run_kernel(ctx, kKSubtreeCheck, v, 1, (int)(lv.size() - li));
             run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm));
+            break;
         }
+        if (v.C == 0) continue;
         run_kernel(ctx, kKPlan, v, 1);
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
         if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
@@ -517,6 +522,31 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         partition_level(ctx, v, true);
         ORB_CUDA(cudaGetLastError());
     }
+    return ORB_OK;
+}
+
+// After the main graph of a build that planned subtrees (sub_from >= 0): waits for it and
+// reads whether the device took the subtree path (*taken). When it refused (a cell too large
+// for one CTA), a second graph runs the level kernels of the levels from sub_from down. The
+// build's end event is recorded again after it.
+orb_status finish_subtree_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv,
+                                 std::vector<uint64_t> key, uint32_t *passes, int sub_from,
+                                 uint64_t max_n, bool *taken) {
+    *taken = false;
+    if (sub_from < 0) return ORB_OK;
+    ORB_CUDA(cudaStreamSynchronize(ctx->stream));
+    uint32_t flag = 0;
+    ORB_CUDA(cudaMemcpy(&flag, ctx->sub_flag.p, sizeof flag, cudaMemcpyDeviceToHost));
+    *taken = flag != 0;
+    if (*taken) return ORB_OK;
+    if (ctx->use_graphs) collect_graph_profile(ctx);  // the main graph's kernel events
+    key.push_back(0x5E57u);  // the levels from sub_from down
+    v.skip = nullptr;
+    orb_status st = run_graphed(ctx, key, passes, [&](uint32_t *pp) -> orb_status {
+        return run_levels(ctx, v, lv, pp, sub_from, max_n, true);
+    });
+    if (st != ORB_OK) return st;
+    ORB_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
     return ORB_OK;
 }
 
@@ -721,15 +751,14 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    bool taken = false;  // the subtree kernel finished the tree
+    st = finish_subtree_levels(ctx, v, lv, key, &passes, sub_from, n, &taken);
+    if (st != ORB_OK) return st;
     bool written = false;  // the subtree kernel wrote the particles to the host arrays
     if (!dev) {
         ORB_CUDA(cudaStreamSynchronize(s));
         ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
-        if (direct) {
-            uint32_t taken = 0;
-            ORB_CUDA(cudaMemcpy(&taken, ctx->sub_flag.p, sizeof taken, cudaMemcpyDeviceToHost));
-            written = taken != 0;
-        }
+        written = direct && taken;
         ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
         if (n && !written) {
             ORB_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -1201,6 +1230,9 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
     });
     if (st != ORB_OK) return st;
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    bool taken = false;
+    st = finish_subtree_levels(ctx, v, lv, key, &passes, sub_from, max_n, &taken);
+    if (st != ORB_OK) return st;
     if (!dev) {
         ORB_CUDA(cudaStreamSynchronize(s));
         ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));

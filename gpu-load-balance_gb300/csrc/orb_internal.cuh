@@ -30,7 +30,10 @@ constexpr int kThreads = 256;
 constexpr int kHistBlocksPerSm = ORB_HIST_BLOCKS_PER_SM;
 constexpr int kTileBlocksPerSm = 4;  // resident CTAs of the one-tile cell bisection
 constexpr int kSubtreeBlocksPerSm = 4;  // CTAs of the subtree kernel per SM (its grid)
-constexpr uint32_t kSubMaxParticles = 17408;  // largest cell one subtree CTA takes
+#ifndef ORB_SUB_MAX
+#define ORB_SUB_MAX 34816  // 2^15 + 2048: a 2^27-particle tree takes its last 4 levels
+#endif
+constexpr uint32_t kSubMaxParticles = ORB_SUB_MAX;  // largest cell one subtree CTA takes
 constexpr int kSubMaxLevels = 6;              // deepest tree one subtree CTA finishes
 
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)

@@ -2339,7 +2339,7 @@ __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split)
 // Subtrees: once every cell of a level holds at most kSubMax particles, one CTA takes a
 // cell and finishes all the levels below it (bisection, Hoare partition and split of each
 // descendant, breadth first), the same steps as the level kernels at CTA scale. A cell's
-// particles (at most 204 KB) stay in L2 across its levels instead of crossing DRAM once per
+// particles (at most 408 KB) stay in L2 across its levels instead of crossing DRAM once per
 // level, and the level kernels of those levels do not run.
 // ------------------------------------------------------------------------------------
 constexpr uint32_t kSubMax = kSubMaxParticles;  // particles of a cell a CTA can take (masks)

@@ -189,9 +189,9 @@ typedef struct orb_tuning {
                                       this many keys per tile, 1..16384 (default 64) */
     uint32_t cta_min_cells;        /* levels with at least this many cells bisect one cell per
                                       CTA; 0 = never (default) */
-    uint32_t subtree_levels;       /* the last levels (at most this many, 0..6, default 3) are
+    uint32_t subtree_levels;       /* the last levels (at most this many, 0..6, default 4) are
                                       finished by one CTA per cell once every cell of a level
-                                      fits one (at most 17408 particles); 0 = never */
+                                      fits one (at most 34816 particles); 0 = never */
     uint32_t predict_sigmas;       /* first count pass of cells of at least 2^18 particles: the
                                       keys are binned only inside a bracket predicted from a
                                       strided sample (its median +- this many standard errors),

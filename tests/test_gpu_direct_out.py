@@ -61,3 +61,26 @@ def test_pinned_outputs_subtree_refused(ctx, oracle):
         a[: n // 2] = np.float32(0.125)
     res = check(ctx, oracle, x, y, z, d, True)
     assert res.info["degenerate_cells"] > 0 or res.info["unfound_cells"] > 0
+
+
+def test_batch_subtree_refused(ctx, oracle):
+    # a batch whose largest instance keeps a cell too large for one CTA at the planned
+    # subtree level: the device refuses the subtree path for the whole batch, and the level
+    # kernels finish every instance (each must still equal the oracle on its own)
+    n0, d0 = 1 << 21, 1 << 12
+    x0, y0, z0 = oracle.gen_uniform(95, n0)
+    for a in (x0, y0, z0):
+        a[: n0 // 2] = np.float32(-0.25)
+    x1, y1, z1 = oracle.gen_plummer(96, 300000)
+    inst = [{"offset": 0, "n": n0, "d": d0, "levels": 0},
+            {"offset": n0, "n": 300000, "d": 1 << 9, "levels": 0}]
+    bx, by, bz = (np.concatenate(p) for p in ((x0, x1), (y0, y1), (z0, z1)))
+    parts, perm, _ = ctx.build_batch(bx, by, bz, inst)
+    for (heap, ranges), ins, (ix, iy, iz) in zip(parts, inst, ((x0, y0, z0), (x1, y1, z1))):
+        ref = oracle.build_tree(ix, iy, iz, ins["d"])
+        a, b = ins["offset"], ins["offset"] + ins["n"]
+        assert heap.tobytes() == ref.heap.tobytes()
+        assert np.array_equal(ranges, ref.ranges[0])
+        assert np.array_equal(perm[a:b], ref.perm)
+        for got, want in ((bx, ref.x), (by, ref.y), (bz, ref.z)):
+            assert np.array_equal(got[a:b].view(np.uint32), want.view(np.uint32))

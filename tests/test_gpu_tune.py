@@ -28,7 +28,7 @@ def fresh(engine):
 def test_get_set_roundtrip_and_limits(fresh, engine):
     d = fresh.get_tuning()
     assert d == dict(hist_blocks_per_sm=6, part_blocks_per_sm=8, tile_blocks_per_sm=4,
-                     sparse_keys_per_tile=64, cta_min_cells=0, subtree_levels=3, predict_sigmas=0)
+                     sparse_keys_per_tile=64, cta_min_cells=0, subtree_levels=4, predict_sigmas=0)
     fresh.set_tuning(part_blocks_per_sm=12, sparse_keys_per_tile=100)
     assert fresh.get_tuning()["part_blocks_per_sm"] == 12
     assert fresh.get_tuning()["sparse_keys_per_tile"] == 100
