@@ -91,6 +91,7 @@ struct orb_ctx {
     DevBuf<uint8_t> warm;
     DevBuf<uint32_t> sub_flag;  // subtree path taken (one word)
     BuildCounters *h_counters = nullptr;  // pinned
+    uint32_t *h_sub_flag = nullptr;       // pinned: the subtree path was taken
 
     // service layer state
     bool loaded = false;
@@ -534,10 +535,10 @@ orb_status finish_subtree_levels(orb_ctx *ctx, Level v, const std::vector<LevelD
                                  uint64_t max_n, bool *taken) {
     *taken = false;
     if (sub_from < 0) return ORB_OK;
+    ORB_CUDA(cudaMemcpyAsync(ctx->h_sub_flag, ctx->sub_flag.p, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             ctx->stream));
     ORB_CUDA(cudaStreamSynchronize(ctx->stream));
-    uint32_t flag = 0;
-    ORB_CUDA(cudaMemcpy(&flag, ctx->sub_flag.p, sizeof flag, cudaMemcpyDeviceToHost));
-    *taken = flag != 0;
+    *taken = *ctx->h_sub_flag != 0;
     if (*taken) return ORB_OK;
     if (ctx->use_graphs) collect_graph_profile(ctx);  // the main graph's kernel events
     key.push_back(0x5E57u);  // the levels from sub_from down
@@ -616,7 +617,8 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             const char *ng = std::getenv("ORB_NO_GRAPHS");
             ctx->use_graphs = !(ng && ng[0] && ng[0] != '0');
         }
-        if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess) {
+        if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess ||
+            (e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_sub_flag), sizeof(uint32_t))) != cudaSuccess) {
             st = cuda_fail(ctx, e, "cudaMallocHost");
             break;
         }
@@ -661,6 +663,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->listed.release(); ctx->cmp_bad.release(); ctx->cmp_off.release(); ctx->cmp_cnt.release();
     ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->h_sub_flag) cudaFreeHost(ctx->h_sub_flag);
     collect_profile(ctx);
     drop_all_graphs(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
