@@ -87,16 +87,6 @@ __device__ __forceinline__ uint32_t block_max(uint32_t v, uint32_t *sh) {
     return warp_max(t);
 }
 
-__device__ __forceinline__ uint32_t block_min(uint32_t v, uint32_t *sh) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    v = warp_min(v);
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    uint32_t t = lane < nw ? sh[lane] : 0xffffffffu;
-    return warp_min(t);
-}
-
 // Exclusive scan of two counters over the block (thread order). Returns the exclusive
 // prefix; *ta, *tb receive the block totals. `sh` holds >= 64 words.
 __device__ __forceinline__ uint2 block_excl_scan2(uint32_t a, uint32_t b, uint32_t *sh,
@@ -704,17 +694,15 @@ constexpr int kHistVec = 4;
 
 constexpr int kGroup = 4 * kHistVec;  // keys a thread holds per round
 
-// The keys [e0, e1) of one tile (at most kTile keys), visited by the CTA's threads. The
-// 16-byte aligned body is read in rounds of kHistVec float4 loads a thread (all issued
-// before any key is used); each key goes through settle(k), branch-free code for the common
-// case that returns false for a key it leaves. Left keys are visited through rest(k)
-// (reloaded): after the tile's last round, from one bit each (Rounds = false: for passes
-// that leave few keys), or right after their own round while its lines are still in L1
-// (Rounds = true: for passes that leave a few percent). The unaligned head and tail go
-// through visit(k). `pad` fills the missing lanes of the last round: settle(pad) must count
-// nothing (a pad it leaves is skipped).
-static_assert(kTile / (4 * kHistVec * kThreads) <= 4, "scan_tile keeps 16 bits a round, 4 rounds");
-template <uint32_t NT, bool Rounds, class Settle, class Rest, class Visit>
+// The keys [e0, e1) of one tile (at most kTile keys), visited by the CTA's threads, for a
+// pass that leaves a few percent of its keys (the sampled pass). The 16-byte aligned body is
+// read in rounds of kHistVec float4 loads a thread (all issued before any key is used); each
+// key goes through settle(k), branch-free code for the common case that returns false for a
+// key it leaves; a round's left keys are visited right after it through rest(k) (reloaded
+// while its lines are still in L1). The unaligned head and tail go through visit(k). `pad`
+// fills the missing lanes of the last round: settle(pad) must count nothing (a pad it leaves
+// is skipped).
+template <uint32_t NT, class Settle, class Rest, class Visit>
 __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32_t e1, float pad,
                                           Settle settle, Rest rest, Visit visit) {
     const uint32_t ti = threadIdx.x;  // NT = blockDim.x
@@ -724,12 +712,7 @@ __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32
     const uint32_t n4 = (e1 - a0) >> 2;
     const float4 *k4 = reinterpret_cast<const float4 *>(keys + a0);
     const float *kb = keys + a0;
-    unsigned long long left = 0;  // Rounds = false: bit 16 r + 4 u + c: component c of load u
-    uint32_t r = 0, j0 = 0;
-    auto take = [&](uint32_t b, uint32_t jr) {  // bit b of round jr
-        const uint32_t j = jr + ((b >> 2) & 3u) * NT + ti;
-        if (j < n4) rest(__ldg(kb + 4 * j + (b & 3u)));  // else a pad lane
-    };
+    uint32_t j0 = 0;
     auto round = [&](auto full) {
         float4 q[kHistVec];
 #pragma unroll
@@ -740,30 +723,22 @@ __device__ __forceinline__ void scan_tile(const float *keys, uint32_t e0, uint32
             else
                 q[u] = j < n4 ? __ldg(k4 + j) : make_float4(pad, pad, pad, pad);
         }
-        uint32_t miss = 0;
+        uint32_t miss = 0;  // bit 4u + c: component c of load u left
 #pragma unroll
         for (int u = 0; u < kHistVec; ++u) {
             const float kk[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
 #pragma unroll
             for (int c = 0; c < 4; ++c) miss |= (uint32_t)!settle(kk[c]) << (4 * u + c);
         }
-        if (Rounds) {
-            while (miss) {
-                const uint32_t b = (uint32_t)__ffs(miss) - 1u;
-                miss &= miss - 1u;
-                take(b, j0);
-            }
-        } else {
-            left |= (unsigned long long)miss << (16u * r);
+        while (miss) {
+            const uint32_t b = (uint32_t)__ffs(miss) - 1u;
+            miss &= miss - 1u;
+            const uint32_t j = j0 + (b >> 2) * NT + ti;
+            if (j < n4) rest(__ldg(kb + 4 * j + (b & 3u)));  // else a pad lane
         }
     };
-    for (; j0 + kHistVec * NT <= n4; j0 += kHistVec * NT, ++r) round(Flag<true>());
+    for (; j0 + kHistVec * NT <= n4; j0 += kHistVec * NT) round(Flag<true>());
     if (j0 < n4) round(Flag<false>());
-    while (left) {
-        const uint32_t b = (uint32_t)(__ffsll((long long)left) - 1);
-        left &= left - 1;
-        take(b, (b >> 4) * (kHistVec * NT));
-    }
     for (uint32_t i = a0 + (n4 << 2) + ti; i < e1; i += NT) visit(__ldg(keys + i));
 }
 
@@ -1227,7 +1202,7 @@ __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
             // buffer holds one tile's keys), keys above it and NaN ignored
             const float pa = s_hc.pa, pb = s_hc.pb;
             auto key = [&](float k) { pred_key(k, &s_hc, s_hist, s_cmp, &s_ncmp, s_edge); };
-            scan_tile<kThreads, true>(
+            scan_tile<kThreads>(
                 keys, e0, e1, s_hc.R,
                 [&](float k) {
                     below += k < pa;
