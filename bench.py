@@ -534,7 +534,7 @@ def gpu_arm(args):
     # count-left (the spec kernel family): every launch that counts keys below a cut in
     # the warm-up steps, against the measured HBM peak; the last levels run inside k_subtree
     # (bisection and partition of one cell per CTA), listed in kernels_per_step_warmup
-    cl_names = [k for k in ("count_left_hist", "bisect_tile", "bisect_warp", "count_left_sample",
+    cl_names = [k for k in ("count_left_hist", "bisect_tile", "count_left_sample",
                             "count_left_sample_pick") if k in warm]
     cl_bytes = sum(warm[k]["bytes"] for k in cl_names) / wsteps
     cl_ms = sum(warm[k]["total_ms"] for k in cl_names) / wsteps

@@ -55,7 +55,6 @@ enum Kernel : int {
     kKGenerate,
     kKBisectCta,
     kKTileMap,
-    kKBisectWarp,  // bytes of the small cells k_bisect_tile bisects in registers (no launch)
     kKBisectTile,
     kKWarmStart,
     kKSubtreeCheck,

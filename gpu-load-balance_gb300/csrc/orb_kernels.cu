@@ -24,7 +24,7 @@ namespace orb {
 const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
-    "tile_map", "bisect_warp", "bisect_tile", "warm_start", "subtree_check", "subtree",
+    "tile_map", "bisect_tile", "warm_start", "subtree_check", "subtree",
     "count_left_sample", "count_left_sample_pick"};
 
 namespace {
@@ -1306,7 +1306,7 @@ __device__ __forceinline__ void bisect_small(const Level &v, int c, uint32_t lan
         v.state[c] = st;
         atomicMax(&v.counters->max_iters, it);
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
-        add_bytes(v, kKBisectWarp, 4ull * n);
+        add_bytes(v, kKBisectTile, 4ull * n);  // the launch that bisects it
     }
 }
 
