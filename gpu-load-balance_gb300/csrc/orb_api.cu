@@ -2,8 +2,9 @@
 //
 // orb_build runs the reference's master() level loop (src/orbit.cpp:102-275) with every
 // step on the device: per level a plan, histogram/resolve passes that replay the
-// bisection, the parallel Hoare partition and the split. The host only launches and, per
-// bisection pass, reads one flag that says whether any cell of the level is still active.
+// bisection, the parallel Hoare partition and the split, and the last levels one CTA per
+// cell. The work is captured in CUDA graphs and replayed; the host reads one flag per build
+// (whether the device took the subtree path for the last levels).
 #include <cuda_runtime.h>
 
 #include <cmath>

@@ -14,6 +14,10 @@
 //              i = min(L_{s+1}, R_s) and swaps (i, n-1). Counts, a per-cell scan, rank
 //              tables and a swap pass reproduce the permutation exactly.
 //   split      src/cell.h:78-126 and src/orbit.cpp:235-250 on the device.
+// Beside them: the bisection of cells of at most one tile in one launch (a warp per cell),
+// the subtree kernel (one CTA finishes a cell's last levels with its particles in L2), the
+// optional sampled first pass, the service count-left, seeded generators and the batched
+// and served forms' helpers.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
