@@ -132,3 +132,60 @@ def test_guess_settles_almost_every_key_of_a_box():
     k = (L + f32(R - L) * rng.random(200000).astype(f32)).astype(f32)
     ok, _ = guess_bin(k, L, R, scale, nb)
     assert ok.mean() > 0.99
+
+
+def near_bin(k, L, scale, e, top):
+    """Restatement of the device's near_bin for keys L <= k < R: the floor of the same guess
+    (its fused multiply-add encoding, clamped to the top leaf), then the guessed leaf or a
+    neighbour checked against the edge table; None where the device falls back to a search."""
+    y = fma_2048((k - f32(L)).astype(f32), scale)
+    t = y.view(np.uint32).astype(np.int64) - 0x45000000  # the encoding of 2048.0f
+    g = np.minimum(t >> 12, top)
+    res = np.full(k.shape, -1, np.int64)
+    below = k < e[g]
+    inside = ~below & (k < e[g + 1])
+    res[inside] = g[inside]
+    lo = below & (g > 0)
+    lo_ok = lo.copy()
+    lo_ok[lo] = ~(k[lo] < e[g[lo] - 1])
+    res[lo_ok] = g[lo_ok] - 1
+    hi = ~below & ~inside & (g < top)
+    hi_ok = hi.copy()
+    hi_ok[hi] = k[hi] < e[g[hi] + 2]
+    res[hi_ok] = g[hi_ok] + 1
+    return res  # -1: the search
+
+
+def test_rejected_keys_need_no_search_when_the_guess_is_trusted():
+    """The exact path of the count pass (near_bin): where the margin lets the guess be trusted
+    (its bins are more than 16 ulps wide) the guessed leaf or a neighbour is the exact leaf,
+    so the edge-table search is never taken; every bin it returns is the exact one."""
+    rng = np.random.default_rng(7)
+    checked = 0
+    for trial in range(300):
+        K = int(rng.integers(4, 12))
+        nb = 1 << K
+        if trial % 2 == 0:
+            L = f32(-0.5 + (rng.integers(0, 1 << 24) * 2.0 ** -24))
+            R = f32(L + f32(2.0 ** -int(rng.integers(0, 20))))
+        else:
+            L = f32(rng.uniform(-1e3, 1e3))
+            R = f32(L + f32(10.0 ** rng.uniform(-5, 2)))
+        if not (L < R) or not np.isfinite(R - L):
+            continue
+        e = midpoint_edges(L, R, K)
+        scale = f32(nb) / f32(R - L)
+        k = (f32(L) + f32(R - L) * rng.random(3000).astype(f32)).astype(f32)
+        j = rng.integers(0, nb + 1, 1000)
+        near = np.concatenate([e[j], np.nextafter(e[j], f32(np.inf)), np.nextafter(e[j], f32(-np.inf))])
+        k = np.concatenate([k, near.astype(f32)])
+        k = k[(k >= L) & (k < R)]
+        exact = np.searchsorted(e[:nb], k, side="right") - 1
+        got = near_bin(k, L, scale, e, nb - 1)
+        found = got >= 0
+        assert np.array_equal(got[found], exact[found]), f"near_bin off in [{L!r}, {R!r}) K={K}"
+        trusted = f32(margin(L, R, scale, max(nb, 2048)) * f32(4096.0)) < 2048
+        if trusted:
+            assert found.all(), f"search needed in a trusted bracket [{L!r}, {R!r}) K={K}"
+            checked += 1
+    assert checked > 50
