@@ -531,9 +531,10 @@ def gpu_arm(args):
         "share_of_kernel_time": round(dom_share, 4),
     }
     wsteps = max(args.warmup, 1)
-    # count-left (the kernel family held to 0.60 of the HBM peak): every launch that counts keys below a cut in
-    # the warm-up steps, against the measured HBM peak; the last levels run inside k_subtree
-    # (bisection and partition of one cell per CTA), listed in kernels_per_step_warmup
+    # count-left (the kernel family held to 0.60 of the HBM peak): every launch that counts
+    # keys below a cut in the warm-up steps, against the measured HBM peak; the last levels
+    # run inside k_subtree (bisection and partition of one cell per CTA), listed in
+    # kernels_per_step_warmup
     cl_names = [k for k in ("count_left_hist", "bisect_tile", "count_left_sample",
                             "count_left_sample_pick") if k in warm]
     cl_bytes = sum(warm[k]["bytes"] for k in cl_names) / wsteps
