@@ -141,6 +141,53 @@ def test_parallel_hoare_matches_loop(oracle):
         assert np.array_equal(perm, p.astype(np.uint32))
 
 
+def test_hoare_children_from_masks(oracle):
+    """What the parallel characterisation tells about a level's children before anything
+    moves (the basis for moving two levels at once): a particle goes to the left child
+    exactly when it is a swapped right partner (position R_k, k < s) or it is not swapped
+    and its position is below i; the left child's order is the cell's, except that position
+    L_k (k < s) holds the particle from R_k. Checked, with the next level's cut applied to
+    the left child, against two passes of the literal loop."""
+    rng = np.random.default_rng(3)
+    checked = 0
+    for _ in range(4000):
+        n = int(rng.integers(0, 40))
+        span = int(rng.integers(1, 6))
+        a = rng.integers(0, span, n).astype(np.float32)
+        b = rng.integers(0, span, n).astype(np.float32)
+        cut = np.float32(rng.integers(-1, span + 1) - 0.5 * rng.integers(0, 2))
+        cut2 = np.float32(rng.integers(-1, span + 1) - 0.5 * rng.integers(0, 2))
+        x, y = a.copy(), b.copy()
+        perm = np.arange(n, dtype=np.uint32)
+        i, dg = oracle.hoare(x, y, np.zeros(n, np.float32), 0, float(cut), perm=perm)
+        if dg:
+            continue  # a clamped cell sends everything left (the engine's own rule)
+        ge, le = ~(a < cut), ~(a > cut)
+        f = np.concatenate([[0], np.cumsum(ge)])
+        g = np.concatenate([np.cumsum(le[::-1])[::-1], [0]])
+        s = int(np.max(np.minimum(f, g)))
+        L, R = np.nonzero(ge)[0][:s], np.nonzero(le)[0][::-1][:s]
+        moved_in, moved_out = np.zeros(n, bool), np.zeros(n, bool)
+        moved_in[R], moved_out[L] = True, True
+        left = moved_in | (~moved_in & ~moved_out & (np.arange(n) < i))
+        truth = np.zeros(n, bool)
+        truth[perm[:i]] = True
+        assert np.array_equal(left, truth)
+        order = np.arange(i)
+        order[L] = R  # L_k < i for k < s
+        assert np.array_equal(order, perm[:i].astype(np.int64))
+        # the next level on the left child, from the keys gathered in that order
+        p1 = np.arange(i, dtype=np.uint32)
+        i1, _ = oracle.hoare(y[:i].copy(), np.zeros(i, np.float32), np.zeros(i, np.float32), 0,
+                             float(cut2), perm=p1)
+        p2 = np.arange(i, dtype=np.uint32)
+        i2, _ = oracle.hoare(b[order].copy(), np.zeros(i, np.float32), np.zeros(i, np.float32), 0,
+                             float(cut2), perm=p2)
+        assert i1 == i2 and np.array_equal(p1, p2)
+        checked += 1
+    assert checked > 2000
+
+
 def test_oracle_digests(oracle):
     with open(os.path.join(GOLDEN, "oracle_builds.json")) as f:
         cases = json.load(f)
