@@ -65,6 +65,11 @@ struct orb_ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // builds from host memory: y and z are copied on copy_stream while the root level (cut
+    // along x) bisects; the first partition waits for yz_ready (yz_pending: not yet waited)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t yz_ready = nullptr;
+    bool yz_pending = false;
     std::string err;
 
     DevBuf<float> x, y, z;
@@ -429,6 +434,10 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     run_kernel(ctx, kKPartClassify, v, g);
     run_kernel(ctx, kKPartScan, v, g, (int)(ctx->pt_ge_pre.cap / 1024 + 1));
     run_kernel(ctx, kKPartCells, v, g);
+    if (ctx->yz_pending) {  // the first kernel that reads y and z
+        cudaStreamWaitEvent(ctx->stream, ctx->yz_ready, ctx->capturing ? cudaEventWaitExternal : 0);
+        ctx->yz_pending = false;
+    }
     run_kernel(ctx, kKPartSwap, v, g);
     run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
 }
@@ -671,6 +680,8 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->yz_ready) cudaEventDestroy(ctx->yz_ready);
     delete ctx;
     return ORB_OK;
 }
@@ -705,6 +716,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     float *dx = x, *dy = y, *dz = z;
     cudaStream_t s = ctx->stream;
     float h2d_ms = 0.f, d2h_ms = 0.f;
+    ctx->yz_pending = false;
     if (!dev) {
         ORB_CUDA(ctx->x.ensure(n + 1));
         ORB_CUDA(ctx->y.ensure(n + 1));
@@ -714,11 +726,20 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         dz = ctx->z.p;
         ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
         if (n) {
+            // x first; y and z on the copy stream, so the root level (cut along x,
+            // src/orbit.cpp:75) bisects while they arrive; its partition waits for them
+            if (!ctx->copy_stream) ORB_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+            if (!ctx->yz_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->yz_ready, cudaEventDisableTiming));
             ORB_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(float), cudaMemcpyHostToDevice, s));
-            ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, s));
-            ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, s));
+            ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[2], 0));
+            ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
+            ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
+            ORB_CUDA(cudaEventRecord(ctx->yz_ready, ctx->copy_stream));
+            ORB_CUDA(cudaEventRecord(ctx->ev[3], ctx->copy_stream));
+            ctx->yz_pending = true;
+        } else {
+            ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
         }
-        ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
     }
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
@@ -746,6 +767,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     if (!direct) v.hx = v.hy = v.hz = nullptr, v.hperm = nullptr;
     for (const void *p : {(const void *)v.hx, (const void *)v.hy, (const void *)v.hz, (const void *)v.hperm})
         key_add(key, p);
+    key.push_back(ctx->yz_pending ? 1u : 0u);  // the graph waits for y and z before the first swap
     uint32_t passes = 0;
     st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
         ctx->launches[kKInit] += 1;
@@ -754,6 +776,11 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         return run_levels(ctx, v, lv, pp, sub_from, n);
     });
     if (st != ORB_OK) return st;
+    if (ctx->yz_pending || (!dev && n)) {
+        // a replayed graph holds the wait; a build without a partition (no levels) waits here
+        ctx->yz_pending = false;
+        ORB_CUDA(cudaStreamWaitEvent(s, ctx->yz_ready, 0));
+    }
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
     bool taken = false;  // the subtree kernel finished the tree
     st = finish_subtree_levels(ctx, v, lv, key, &passes, sub_from, n, &taken);
@@ -1071,6 +1098,7 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
                                    uint32_t flags, orb_build_info *info) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
+    ctx->yz_pending = false;  // batched builds copy their inputs before the build
     if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
     if ((n_total > 0 && (!x || !y || !z)) || (k > 0 && (!inst || !heaps || !ranges)))
         return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
