@@ -146,8 +146,10 @@ def test_hoare_children_from_masks(oracle):
     moves (the basis for moving two levels at once): a particle goes to the left child
     exactly when it is a swapped right partner (position R_k, k < s) or it is not swapped
     and its position is below i; the left child's order is the cell's, except that position
-    L_k (k < s) holds the particle from R_k. Checked, with the next level's cut applied to
-    the left child, against two passes of the literal loop."""
+    L_k (k < s) holds the particle from R_k; the right child's is the cell's, except that
+    position R_k holds the particle from L_k, and then positions i and n-1 exchange. Checked,
+    with the next level's cut applied to the left child, against two passes of the literal
+    loop."""
     rng = np.random.default_rng(3)
     checked = 0
     for _ in range(4000):
@@ -176,6 +178,13 @@ def test_hoare_children_from_masks(oracle):
         order = np.arange(i)
         order[L] = R  # L_k < i for k < s
         assert np.array_equal(order, perm[:i].astype(np.int64))
+        # the right child: position R_k (>= i) holds the particle from L_k, then positions i
+        # and n-1 exchange (the final swap)
+        right = np.arange(i, n)
+        right[R - i] = L
+        if i < n:
+            right[[0, n - 1 - i]] = right[[n - 1 - i, 0]]
+        assert np.array_equal(right, perm[i:].astype(np.int64))
         # the next level on the left child, from the keys gathered in that order
         p1 = np.arange(i, dtype=np.uint32)
         i1, _ = oracle.hoare(y[:i].copy(), np.zeros(i, np.float32), np.zeros(i, np.float32), 0,
