@@ -58,6 +58,7 @@ int log2_exact(uint32_t d) {
     return k;
 }
 
+
 }  // namespace
 
 struct orb_ctx {
@@ -78,6 +79,11 @@ struct orb_ctx {
     DevBuf<uint2> ranges;
     DevBuf<uint32_t> tile_off, hist_off, below, inb, part_s, part_i, part_le, out_counts;
     DevBuf<uint32_t> htile_cell, ptile_cell;
+    // test hooks (orb_test_set_scan_wait): polls of a look-back wait, and the value the
+    // tile scan's block ticket starts from (0 normally; 1 leaves the first block's status
+    // unpublished, so its successor's wait runs out)
+    uint32_t spin_limit = kLookbackSpinLimit;
+    uint32_t scan_ticket_start = 0;
     // launch tuning (orb_set_tuning / orb_autotune_batch); cta_min_cells = 0 means never
     orb_tuning tune = {(uint32_t)kHistBlocksPerSm, 8u, (uint32_t)kTileBlocksPerSm, 64u, 0u, 4u, 0u};
     DevBuf<uint8_t> hist_k, state, iters, listed, cmp_bad;
@@ -259,6 +265,7 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.part_le = ctx->part_le.p;
     v.out_counts = ctx->out_counts.p;
     v.sparse_per_tile = ctx->tune.sparse_keys_per_tile;
+    v.spin_limit = ctx->spin_limit;
     v.counters = ctx->counters.p;
     return v;
 }
@@ -419,6 +426,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
         key_add(key, p);
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
+    key.push_back(((uint64_t)ctx->spin_limit << 8) | ctx->scan_ticket_start);
     for (uint32_t t : {ctx->tune.hist_blocks_per_sm, ctx->tune.part_blocks_per_sm, ctx->tune.tile_blocks_per_sm,
                        ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells, ctx->tune.subtree_levels,
                        ctx->tune.predict_sigmas})
@@ -431,6 +439,8 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
     // look-back state of the tile scan: status words cleared, ticket at zero
     cudaMemsetAsync(ctx->pt_status.p, 0, ctx->pt_status.cap * sizeof(unsigned long long), ctx->stream);
     cudaMemsetAsync(&ctx->counters.p->ticket, 0, sizeof(uint32_t), ctx->stream);
+    if (ctx->scan_ticket_start)  // test hook: the low byte (little-endian) of the ticket
+        cudaMemsetAsync(&ctx->counters.p->ticket, (int)ctx->scan_ticket_start, 1, ctx->stream);
     run_kernel(ctx, kKPartClassify, v, g);
     run_kernel(ctx, kKPartScan, v, g, (int)(ctx->pt_ge_pre.cap / 1024 + 1));
     run_kernel(ctx, kKPartCells, v, g);
@@ -695,13 +705,15 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
     if ((n > 0 && (!x || !y || !z)) || !heap || !ranges || !lower || !upper)
         return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
-    if (d == 0 || (d & (d - 1)) != 0)
-        return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "d must be a power of two");
+    if (d == 0) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "d must be at least 1");
     if (n >= (1ull << 31)) return fail(ctx, ORB_ERR_CAPACITY, "n must be below 2^31");
     if (d > (1u << 30)) return fail(ctx, ORB_ERR_CAPACITY, "d too large");
-    const int ylev = log2_exact(d);
-    if (levels == 0) levels = (uint32_t)ylev;
-    if ((int)levels > ylev) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "levels exceeds log2(d)");
+    const Slices sl(d);
+    if (levels == 0) levels = sl.max_levels();
+    if (levels > sl.max_levels())
+        return fail(ctx, ORB_ERR_INVALID_ARGUMENT,
+                    "levels exceeds log2(d) (d a power of two) or the reference's bound "
+                    "ceil(log2 d) - 1 (other d)");
     const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
     if (dev && n > 0 && (!is_device_ptr(x) || !is_device_ptr(y) || !is_device_ptr(z) ||
                          (perm && !is_device_ptr(perm))))
@@ -709,7 +721,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
 
     ORB_CUDA(cudaSetDevice(ctx->device));
     const uint32_t heap_cells = 2 * d - 1;
-    const uint32_t max_cells = levels ? (1u << (levels - 1)) : 1u;
+    uint32_t max_cells = 1;
+    for (uint32_t l = 1; l <= levels; ++l) max_cells = std::max(max_cells, (uint32_t)sl.count(l));
     orb_status st = ensure_level_buffers(ctx, n, max_cells, heap_cells);
     if (st != ORB_OK) return st;
     ORB_CUDA(ctx->idx.ensure(n + 1));
@@ -746,7 +759,7 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
     if (!perm) v.idx = nullptr;  // no permutation asked for: only x, y, z move
     std::vector<LevelDesc> lv;
     for (uint32_t l = 1; l <= levels; ++l)
-        lv.push_back({(1 << (l - 1)) - 1, nullptr, 1 << (l - 1)});  // src/orbit.cpp:104-107
+        lv.push_back({sl.first(l), nullptr, sl.count(l)});  // src/orbit.cpp:104-107
     std::vector<uint64_t> key = level_key(ctx, v);
     key.push_back(0xB111D);  // single build
     key.push_back(n);
@@ -756,7 +769,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
         key_add_f(key, lower[a]);
         key_add_f(key, upper[a]);
     }
-    const int sub_from = subtree_from(ctx, lv, n, levels == (uint32_t)ylev);
+    // subtrees finish complete trees only: d a power of two, built to its leaves
+    const int sub_from = subtree_from(ctx, lv, n, sl.pow2 && levels == sl.depth);
     if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
     key.push_back((uint64_t)(int64_t)sub_from);
     // pinned host outputs of a build that plans subtrees: the subtree kernel writes every
@@ -1115,12 +1129,14 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
     std::vector<std::pair<uint64_t, uint64_t>> spans;
     for (uint32_t i = 0; i < k; ++i) {
         const orb_batch_instance &b = inst[i];
-        if (b.d == 0 || (b.d & (b.d - 1)) != 0 || b.d > (1u << 30))
-            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance d must be a power of two");
+        if (b.d == 0 || b.d > (1u << 30))
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance d must be in [1, 2^30]");
         if (b.offset + b.n > n_total) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance outside the arrays");
-        const int ylev = log2_exact(b.d);
-        const uint32_t L = b.levels ? b.levels : (uint32_t)ylev;
-        if ((int)L > ylev) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "instance levels exceeds log2(d)");
+        const Slices sl(b.d);
+        const uint32_t L = b.levels ? b.levels : sl.max_levels();
+        if (L > sl.max_levels())
+            return fail(ctx, ORB_ERR_INVALID_ARGUMENT,
+                        "instance levels exceeds log2(d) (d a power of two) or ceil(log2 d) - 1");
         lev[i] = L;
         max_levels = std::max(max_levels, L);
         BatchRoot &r = roots[i];
@@ -1148,8 +1164,9 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
         lv_off.push_back(slots.size());
         for (uint32_t i = 0; i < k; ++i) {
             if (lev[i] < l) continue;
-            const int first = (int)roots[i].heap_base + (1 << (l - 1)) - 1;
-            for (int j = 0; j < (1 << (l - 1)); ++j) slots.push_back(first + j);
+            const Slices sl(inst[i].d);
+            const int first = (int)roots[i].heap_base + sl.first(l);
+            for (int j = 0; j < sl.count(l); ++j) slots.push_back(first + j);
         }
         max_cells = std::max<uint32_t>(max_cells, (uint32_t)(slots.size() - lv_off.back()));
     }
@@ -1244,7 +1261,8 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
     bool full = true;
     uint64_t max_n = 0;
     for (uint32_t i = 0; i < k; ++i) {
-        full = full && lev[i] == (uint32_t)log2_exact(inst[i].d);
+        const Slices sl(inst[i].d);
+        full = full && sl.pow2 && lev[i] == sl.depth;
         max_n = std::max<uint64_t>(max_n, inst[i].n);
     }
     const int sub_from = subtree_from(ctx, lv, max_n, full);
@@ -1294,7 +1312,7 @@ static orb_status build_batch_impl(orb_ctx *ctx, float *x, float *y, float *z, u
         return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up or a bisection did not finish");
     // ranges relative to each instance (cells the build filled)
     for (uint32_t i = 0; i < k; ++i) {
-        const uint64_t filled = (2ull << lev[i]) - 1;
+        const uint64_t filled = Slices(inst[i].d).filled(lev[i]);
         uint32_t *r = ranges + 2ull * roots[i].heap_base;
         for (uint64_t j = 0; j < 2 * filled; ++j) r[j] -= roots[i].offset;
     }
@@ -1365,6 +1383,15 @@ orb_status orb_build_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n
     }
     return orb_build_batch_warm(ctx, x, y, z, n, &b, 1, prev_heap, &width, heap_out, ranges_out, perm,
                                 flags, info);
+}
+
+orb_status orb_test_set_scan_wait(orb_ctx *ctx, uint32_t spin_limit, uint32_t ticket_start) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    ctx->err.clear();
+    if (ticket_start > 255) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "ticket_start above 255");
+    ctx->spin_limit = spin_limit ? spin_limit : kLookbackSpinLimit;
+    ctx->scan_ticket_start = ticket_start;
+    return ORB_OK;
 }
 
 orb_status orb_get_tuning(orb_ctx *ctx, orb_tuning *out) {

@@ -5,7 +5,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "orb/orb.h"
+#include "orb_leaf_ratio.h"
 
 namespace orb {
 
@@ -39,6 +42,9 @@ constexpr int kSubMaxLevels = 6;              // deepest tree one subtree CTA fi
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
 constexpr int kWarpKeys = 1024;      // cells up to this size bisect in one warp's registers
+// Polls of a decoupled look-back wait (64 ns apart) before it gives up: about 0.3 s, far
+// beyond any real wait; the kernel then flags the error and finishes its work.
+constexpr uint32_t kLookbackSpinLimit = 1u << 22;
 
 // Kernel kinds, for launch counting, event timing and algorithmic-byte accounting.
 enum Kernel : int {
@@ -132,6 +138,7 @@ struct Level {
     uint32_t *part_le;      // [C] keys <= cut in the cell
     uint32_t *out_counts;   // service calls: per-cell result
     uint32_t sparse_per_tile;  // count pass: sparse once the bracket holds <= this x tiles keys
+    uint32_t spin_limit;    // polls of one look-back wait before it gives up (error flag)
     // warm builds (null otherwise): per heap slot the previous tree's cut and w x its extent
     // (x NaN: no hint) and that tree's cut axis
     const float2 *hint;     // (cut, w x extent) from the previous tree
@@ -159,10 +166,12 @@ __device__ __forceinline__ float mid_cut(float lo, float hi) {
     return __fmul_rn(__fadd_rn(hi, lo), 0.5f);
 }
 
-// src/orbit.cpp:204-208 for an even nLeafCells (ratio = 0.5f exactly; d is a power of two,
-// so every bisected cell has an even leaf count). Returns 0 found, +1 right margin, -1 left.
-__device__ __forceinline__ int convergence(uint32_t count_left, uint32_t count) {
-    float prod = __fmul_rn(__uint2float_rn(count), 0.5f);
+// src/orbit.cpp:204-208: difference = int(float(cl) - float(c) * ratio), found when
+// |difference| < 3, else the right margin moves for a positive difference and the left one
+// otherwise. ratio = leaf_ratio(nLeafCells) (0.5f when the leaf count is even). The
+// uint->float roundings above 2^24 are kept. Returns 0 found, +1 right margin, -1 left.
+__device__ __forceinline__ int convergence(uint32_t count_left, uint32_t count, float ratio) {
+    float prod = __fmul_rn(__uint2float_rn(count), ratio);
     float diff = __fsub_rn(__uint2float_rn(count_left), prod);
     int difference = __float2int_rz(diff);
     if (difference > -3 && difference < 3) return 0;
@@ -172,6 +181,40 @@ __device__ __forceinline__ int convergence(uint32_t count_left, uint32_t count) 
 __device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {
     return axis == 0 ? v.x : (axis == 1 ? v.y : v.z);
 }
+
+// Level slices of the reference's driver for a root of d leaves (src/orbit.cpp:104-107,
+// src/cell.h:65-72): level l (from 1) takes the heap cells [2^(l-1)-1, b_l] with
+// b_l = min(getNCellsOnLastLevel(), 2^l) - 2, getNCellsOnLastLevel() = 2d - 2^ceil(log2 d).
+// For a power of two that is every cell of the level. For other d the reference's loop
+// stops at getNLevels() - 1 = ceil(log2 d) - 1, and a slice may come out partial or empty
+// (b_l < 2^(l-1)-1; the reference then calls its services with a non-positive cell count,
+// which is undefined; here such a level has no cells).
+struct Slices {
+    uint32_t depth;  // getNLevels()
+    uint32_t last;   // getNCellsOnLastLevel()
+    bool pow2;
+    explicit Slices(uint32_t d) {
+        depth = 0;
+        while ((1ull << depth) < d) ++depth;
+        last = (uint32_t)(2ull * d - (1ull << depth));
+        pow2 = (d & (d - 1)) == 0;
+    }
+    // most split levels: log2(d) for a power of two, else the reference's bound
+    uint32_t max_levels() const { return pow2 ? depth : (depth ? depth - 1 : 0); }
+    int first(uint32_t l) const { return (1 << (l - 1)) - 1; }
+    int count(uint32_t l) const {
+        const int b = (int)std::min<uint64_t>(last, 1ull << l) - 2;
+        return std::max(0, b - first(l) + 1);
+    }
+    // heap cells a build of `levels` levels fills: ids [0, 2 b + 3) for the last level with
+    // cells (children 2b+1, 2b+2 of its last cell b), the root alone without levels
+    uint64_t filled(uint32_t levels) const {
+        uint64_t f = 1;
+        for (uint32_t l = 1; l <= levels; ++l)
+            if (count(l) > 0) f = 2ull * (uint64_t)(first(l) + count(l) - 1) + 3;
+        return f;
+    }
+};
 
 // Root of one instance of a batched build.
 struct BatchRoot {

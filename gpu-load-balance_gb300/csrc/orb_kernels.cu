@@ -278,8 +278,9 @@ __global__ void k_init_batch(Level v, const BatchRoot *roots, int k) {
 // Warm builds: whether a hinted bracket [L, R) can hold the cut the bisection looks for,
 // given the counts of keys below L and below R. Outside it every tested cut would keep
 // moving the same margin: count(< L) already too high, or count(< R) still too low.
-__device__ __forceinline__ bool warm_bracket_holds(uint32_t below_L, uint32_t below_R, uint32_t n) {
-    return convergence(below_L, n) <= 0 && convergence(below_R, n) >= 0;
+__device__ __forceinline__ bool warm_bracket_holds(uint32_t below_L, uint32_t below_R, uint32_t n,
+                                                   float ratio) {
+    return convergence(below_L, n, ratio) <= 0 && convergence(below_R, n, ratio) >= 0;
 }
 
 // Restart of a cell whose hinted bracket missed: the reference's own start, the cell's extent
@@ -1257,6 +1258,7 @@ __device__ __forceinline__ void bisect_small(const Level &v, int c, uint32_t lan
     orb_cell_t &cell = v.heap[slot];
     const uint2 rg = v.ranges[slot];
     const uint32_t n = rg.y - rg.x;
+    const float ratio = leaf_ratio(cell.nLeafCells);  // src/orbit.cpp:204
     const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
     float k[kWarpKeysPerLane];
 #pragma unroll
@@ -1273,7 +1275,7 @@ __device__ __forceinline__ void bisect_small(const Level &v, int c, uint32_t lan
             bl += k[j] < L;
             br += k[j] < R;
         }
-        if (!warm_bracket_holds(warp_sum(bl), warp_sum(br), n)) {
+        if (!warm_bracket_holds(warp_sum(bl), warp_sum(br), n, ratio)) {
             const int a = eff_axis(cell.cutAxis);
             L = cell.lower[a];
             R = cell.upper[a];
@@ -1294,7 +1296,7 @@ __device__ __forceinline__ void bisect_small(const Level &v, int c, uint32_t lan
         for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
         cnt = warp_sum(cnt);
         ++it;
-        const int dir = convergence(cnt, n);
+        const int dir = convergence(cnt, n, ratio);
         if (dir == 0)
             st = kFound;
         else if (dir > 0)
@@ -1339,6 +1341,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
         orb_cell_t &cell = v.heap[slot];
         const uint2 rg = v.ranges[slot];
         const uint32_t n = rg.y - rg.x;
+        const float ratio = leaf_ratio(cell.nLeafCells);  // src/orbit.cpp:204
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
         float L = cell.cutMarginLeft, R = cell.cutMarginRight;
         uint32_t it = 0, cand = n;
@@ -1379,7 +1382,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
                         for (int q = 0; q < kListPerLane; ++q) cnt += (q < (int)nk) && kl[q] < cut;
                         const uint32_t cl = below + warp_sum(cnt);
                         ++it;
-                        const int dir = convergence(cl, n);
+                        const int dir = convergence(cl, n, ratio);
                         if (dir == 0)
                             st = kFound;
                         else if (dir > 0)
@@ -1423,7 +1426,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
             __syncwarp();
             if (warm) {
                 warm = false;
-                if (!warm_bracket_holds(below, below + tot, n)) {  // restart on the extent
+                if (!warm_bracket_holds(below, below + tot, n, ratio)) {  // restart on the extent
                     const int a = eff_axis(cell.cutAxis);
                     L = cell.lower[a];
                     R = cell.upper[a];
@@ -1443,7 +1446,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
                 const uint32_t half = width >> 1;
                 const uint32_t cl = below + bins[pos + half];
                 ++it;
-                const int dir = convergence(cl, n);
+                const int dir = convergence(cl, n, ratio);
                 if (dir == 0) {
                     st = kFound;
                     break;
@@ -1488,6 +1491,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
     orb_cell_t &cell = v.heap[slot];
     const uint2 rg = v.ranges[slot];
     const uint32_t n = rg.y - rg.x;
+    const float ratio = leaf_ratio(cell.nLeafCells);  // src/orbit.cpp:204
     const int K = v.hist_k[c];
     uint32_t *g = v.hist + v.hist_off[c];
     float L = cell.cutMarginLeft, R = cell.cutMarginRight;
@@ -1536,7 +1540,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         // sampled pass: prefix = keys below e(lo), the bins hold the keys of [e(lo), e(hi));
         // the replay below is exact when the cut lies between them (see k_sample_bin)
         const uint32_t tot = sum_bins(0, 1u << K);
-        const bool holds = convergence(prefix, n) < 0 && convergence(prefix + tot, n) > 0;
+        const bool holds = convergence(prefix, n, ratio) < 0 && convergence(prefix + tot, n, ratio) > 0;
         __syncwarp();
         if (!holds) {
             for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
@@ -1559,7 +1563,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         const uint32_t h0 = 1u << (K - 1);
         const uint32_t lo = sum_bins(0, h0), hi = sum_bins(h0, h0);
         first_half = lo;
-        const bool holds = warm_bracket_holds(prefix, prefix + lo + hi, n);
+        const bool holds = warm_bracket_holds(prefix, prefix + lo + hi, n, ratio);
         __syncwarp();
         if (!holds) {
             for (uint32_t b = lane; b < (1u << K); b += 32) g[b] = 0u;
@@ -1586,7 +1590,7 @@ __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
         const uint32_t sum = step == 0 && first_half != 0xffffffffu ? first_half : sum_bins(pos, half);
         const uint32_t cl = prefix + sum;
         ++it;
-        const int dir = convergence(cl, n);
+        const int dir = convergence(cl, n, ratio);
         if (dir == 0) {
             st = kFound;
             break;
@@ -1667,6 +1671,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
         orb_cell_t &cell = v.heap[slot];
         const uint2 rg = v.ranges[slot];
         const uint32_t n = rg.y - rg.x;
+        const float ratio = leaf_ratio(cell.nLeafCells);  // src/orbit.cpp:204
         const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
         float L = cell.cutMarginLeft, R = cell.cutMarginRight;
         uint32_t it = 0, base = 0, m = n, inb = n;
@@ -1728,7 +1733,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
                 const uint32_t half = width >> 1;
                 const uint32_t cl = below + s_hist[pos + half];
                 ++it;
-                const int dir = convergence(cl, n);
+                const int dir = convergence(cl, n, ratio);
                 if (dir == 0) {
                     st = kFound;
                     break;
@@ -1848,7 +1853,6 @@ __device__ __forceinline__ float cell_cut(const orb_cell_t &c) {
 constexpr unsigned long long kStAggregate = 1ull << 62;
 constexpr unsigned long long kStInclusive = 2ull << 62;
 constexpr unsigned long long kStFlags = 3ull << 62;
-constexpr uint32_t kLookbackSpinLimit = 1u << 22;
 
 __device__ __forceinline__ unsigned long long pack_status(unsigned long long flag, uint32_t g,
                                                           uint32_t l) {
@@ -1958,7 +1962,7 @@ __global__ void __launch_bounds__(kScanBlock) k_tile_scan(Level v) {
                 if (jj >= 0) {
                     uint32_t spins = 0;
                     while (((st = status[jj]) & kStFlags) == 0ull) {
-                        if (++spins > kLookbackSpinLimit) {
+                        if (++spins > v.spin_limit) {
                             atomicExch(&v.counters->error, 1u);
                             st = kStInclusive;
                             break;
@@ -2037,11 +2041,19 @@ __device__ uint32_t warp_select(const uint32_t *bits, const uint32_t *pre, uint3
     return __shfl_sync(0xffffffffu, pos, __ffs(who) - 1);
 }
 
+// A look-back wait of the tile scan (or a bisection) gave up and flagged the build: the tile
+// prefixes may be incomplete, so the kernels that read them do nothing and the build
+// returns ORB_ERR_TIMEOUT.
+__device__ __forceinline__ bool scan_failed(const Level &v) {
+    return *(volatile const uint32_t *)&v.counters->error != 0u;
+}
+
 // P3: per cell (one warp): totals, the swap count s and the split index i.
 //   s = max_x min(f(x), g(x)), f(x) = #{>= cut in [0,x)}, g(x) = #{<= cut in [x,n)}
 //   i = min(L_{s+1}, R_s); i == n marks the clamped case (every key below the cut).
 __global__ void __launch_bounds__(kThreads) k_part_cells(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= v.C) return;
@@ -2173,6 +2185,7 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #endif
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     __shared__ uint32_t posL[kPTile];
     __shared__ uint32_t posR[kPTile];
     __shared__ uint32_t sh[96];
@@ -2309,6 +2322,7 @@ __device__ void finish_cell(const Level &v, int slot, uint32_t i, bool do_split)
 // P5: finish_cell for every cell of the level.
 __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
+    if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= v.C) return;
     finish_cell(v, level_slot(v, c), v.part_i[c], do_split != 0);
@@ -2389,6 +2403,8 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
     orb_cell_t &cell = v.heap[slot];
     const uint2 rg = v.ranges[slot];
     const uint32_t n = rg.y - rg.x;
+    // subtrees run for d a power of two only: every cell below has an even leaf count
+    const float ratio = 0.5f;  // leaf_ratio(cell.nLeafCells), src/orbit.cpp:204
     const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
     const uint32_t tid = threadIdx.x, lane = tid & 31;
     float L = cell.cutMarginLeft, R = cell.cutMarginRight;
@@ -2413,7 +2429,7 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
                 for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
                 cnt = warp_sum(cnt);
                 ++it;
-                const int dir = convergence(cnt, n);
+                const int dir = convergence(cnt, n, ratio);
                 if (dir == 0)
                     st = kFound;
                 else if (dir > 0)
@@ -2466,7 +2482,7 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
                 const uint32_t half = width >> 1;
                 const uint32_t cl = below + sm.bins[pos + half];
                 ++it;
-                const int dir = convergence(cl, n);
+                const int dir = convergence(cl, n, ratio);
                 if (dir == 0) {
                     st = kFound;
                     break;
@@ -2514,7 +2530,7 @@ __device__ void sub_bisect(const Level &v, int slot, SubSmem &sm, unsigned long 
                         for (int q = 0; q < kPer; ++q) c += kl[q] < cut;
                         const uint32_t cl = below_L + warp_sum(c);
                         ++it;
-                        const int dir = convergence(cl, n);
+                        const int dir = convergence(cl, n, ratio);
                         if (dir == 0)
                             st = kFound;
                         else if (dir > 0)

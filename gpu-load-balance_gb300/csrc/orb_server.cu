@@ -335,9 +335,8 @@ orb_status submit(orb_server *sv, std::unique_ptr<Req> r, uint64_t *request_id) 
 
 orb_status new_instance(orb_server *sv, uint64_t n, uint32_t d, uint32_t levels, const float lower[3],
                         const float upper[3], std::unique_ptr<Req> &r, uint64_t *request_id) {
-    if (d == 0 || (d & (d - 1)) != 0) return ORB_ERR_INVALID_ARGUMENT;
-    uint32_t ylev = 0;
-    while ((1u << ylev) < d) ++ylev;
+    if (d == 0 || d > (1u << 30)) return ORB_ERR_INVALID_ARGUMENT;
+    const uint32_t ylev = orb::Slices(d).max_levels();
     if (levels > ylev) return ORB_ERR_INVALID_ARGUMENT;
     if (n > sv->arena_cap) return ORB_ERR_CAPACITY;  // can never be admitted
     std::lock_guard<std::mutex> lk(sv->mu);

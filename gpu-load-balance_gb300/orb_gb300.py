@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liborb_gb300.so")
 SOURCES = ["orb_kernels.cu", "orb_api.cu", "orb_static.cu", "orb_server.cu"]
-HEADERS = ["orb_internal.cuh"]
+HEADERS = ["orb_internal.cuh", "orb_leaf_ratio.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
@@ -68,7 +68,7 @@ EXPORTS = [
     "orb_server_submit_generate", "orb_server_submit_rebalance", "orb_server_wait", "orb_server_poll",
     "orb_server_fetch", "orb_server_release", "orb_server_get_stats", "orb_get_tuning",
     "orb_set_tuning", "orb_autotune_batch", "orb_build_batch_warm", "orb_build_warm",
-    "orb_server_submit_rebalance_warm",
+    "orb_server_submit_rebalance_warm", "orb_test_set_scan_wait",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -287,6 +287,8 @@ def load(path: str | None = None):
     L.orb_server_release.argtypes = [vp, u64]
     L.orb_server_get_stats.restype = ctypes.c_int
     L.orb_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.orb_test_set_scan_wait.restype = ctypes.c_int
+    L.orb_test_set_scan_wait.argtypes = [vp, u32, u32]
     L.orb_count_left_static.restype = ctypes.c_int
     L.orb_count_left_static.argtypes = [vp, vp, vp, u64, vp, u32, vp, u32, vp, vp]
     _lib = L
@@ -438,6 +440,10 @@ class Context:
             bases.append(heap_cells)
             heap_cells += 2 * b.d - 1
         return arr, heap_cells, bases
+
+    def test_set_scan_wait(self, spin_limit: int = 0, ticket_start: int = 0):
+        """Test hook of the tile scan's bounded look-back wait (orb_test_set_scan_wait)."""
+        self._check(self.lib.orb_test_set_scan_wait(self.h, spin_limit, ticket_start))
 
     # launch tuning -----------------------------------------------------------------
     def get_tuning(self) -> dict:

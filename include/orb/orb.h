@@ -36,7 +36,7 @@ extern "C" {
 
 typedef enum orb_status {
     ORB_OK = 0,
-    ORB_ERR_INVALID_ARGUMENT = 1, /* null pointer, d not a power of two, levels > log2(d) ... */
+    ORB_ERR_INVALID_ARGUMENT = 1, /* null pointer, d = 0, levels beyond the most for d ... */
     ORB_ERR_CUDA = 2,             /* a CUDA runtime call failed; see orb_last_error */
     ORB_ERR_OUT_OF_MEMORY = 3,    /* a device or pinned allocation failed */
     ORB_ERR_CAPACITY = 4,         /* the request exceeds a limit of the engine */
@@ -104,10 +104,18 @@ const char *orb_last_error(const orb_ctx *ctx);
 int orb_abi_version(void);
 
 /*
- * Build the ORB tree of n particles into d leaf cells (d a power of two).
+ * Build the ORB tree of n particles into d leaf cells (1 <= d <= 2^30).
  *   x, y, z   n coordinates each, partitioned in place (reference order after the build)
- *   levels    split levels: 0 selects log2(d) (d leaves); log2(d)-1 is the reference
- *             driver's own loop bound (src/orbit.cpp:102) and gives d/2 leaves
+ *   levels    split levels. Level l splits the heap cells [2^(l-1)-1, min(2d - 2^D, 2^l) - 2],
+ *             D = ceil(log2 d) (the reference's slices, src/orbit.cpp:104-107 with
+ *             src/cell.h:65-72); a cell of k leaves gives ceil(k/2) to its left child
+ *             (src/cell.h:79) and its bisection tests against ratio ceil(k/2)/k
+ *             (src/orbit.cpp:204).
+ *             d a power of two: 0 selects log2(d) (d leaves); log2(d)-1 is the reference
+ *             driver's own loop bound (src/orbit.cpp:102) and gives d/2 leaves.
+ *             Other d: at most the reference's bound D-1, which 0 selects (its slices name
+ *             no complete level below it; a slice that comes out empty is a level without
+ *             cells, where the reference's services are called with a non-positive count).
  *   lower, upper  root box (the reference uses [-0.5,0.5]^3, src/orbit.cpp:45-46)
  *   heap      out: 2d-1 cells; cells deeper than `levels` are zeroed
  *   ranges    out: 2*(2d-1) uint32, {begin,end} per heap cell (cellToRangeMap)
@@ -137,8 +145,8 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
 typedef struct orb_batch_instance {
     uint64_t offset;
     uint64_t n;
-    uint32_t d;      /* leaf cells, a power of two */
-    uint32_t levels; /* 0 = log2(d) */
+    uint32_t d;      /* leaf cells, 1 .. 2^30 */
+    uint32_t levels; /* 0 = the most for d (as orb_build) */
     float lower[3];
     float upper[3];
 } orb_batch_instance;
@@ -363,6 +371,19 @@ orb_status orb_count_left_static(const float *x, const float *y, const float *z,
                                  const orb_cell_t *cells, uint32_t n_cells,
                                  const uint32_t *ranges, uint32_t n_ranges, uint32_t *out,
                                  void *stream);
+
+/*
+ * Test hook of the bounded device waits (no counterpart in the reference, whose errors end
+ * the process, src/constants.h:19-23). The partition's tile scan chains its blocks with a
+ * decoupled look-back; each wait polls a predecessor's status at most spin_limit times
+ * (0 = the default, about 2^22 polls), then flags the build and gives up: the kernels that
+ * would read the scan's prefixes do nothing and the build returns ORB_ERR_TIMEOUT. The
+ * context stays usable. ticket_start (0..255, normally 0) is the value the scan's block
+ * ticket starts from: 1 means no block takes the first status slot, so its successor's
+ * wait runs out, a wait that can never end made into one that ends in a bounded time.
+ * Settings stay until changed; (0, 0) restores the defaults.
+ */
+orb_status orb_test_set_scan_wait(orb_ctx *ctx, uint32_t spin_limit, uint32_t ticket_start);
 
 #ifdef __cplusplus
 }

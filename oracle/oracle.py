@@ -92,7 +92,11 @@ def lib():
         L.oracle_build.argtypes = [fp, fp, fp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
                                    fp, fp, ctypes.c_void_p, u32p, u32p,
                                    ctypes.POINTER(ctypes.c_uint8), ctypes.c_int, ctypes.c_int,
-                                   ctypes.POINTER(_Stats)]
+                                   ctypes.c_int, ctypes.POINTER(_Stats)]
+        L.oracle_level_shape.restype = None
+        L.oracle_level_shape.argtypes = [ctypes.c_uint32, u32p, u32p]
+        L.oracle_max_levels.restype = ctypes.c_uint32
+        L.oracle_max_levels.argtypes = [ctypes.c_uint32]
         _lib = L
     return _lib
 
@@ -166,15 +170,29 @@ class OracleResult:
     stats: dict
 
 
+def level_shape(d: int):
+    """(getNLevels(), getNCellsOnLastLevel()) of a root of d leaves (src/cell.h:65-72)."""
+    a, b = ctypes.c_uint32(), ctypes.c_uint32()
+    lib().oracle_level_shape(d, ctypes.byref(a), ctypes.byref(b))
+    return int(a.value), int(b.value)
+
+
+def max_levels(d: int) -> int:
+    """Most split levels of a build of d leaves: log2(d) for a power of two, else the
+    reference's own bound getNLevels() - 1."""
+    return int(lib().oracle_max_levels(d))
+
+
 def build_tree(x, y, z, d: int, levels: int | None = None, lower=(-0.5, -0.5, -0.5),
                upper=(0.5, 0.5, 0.5), nranks: int = 1, make_axis: bool = False,
-               copy: bool = True, want_perm: bool = True) -> OracleResult:
-    """Run the oracle ORB build. Inputs are copied unless copy=False (then permuted in place)."""
+               copy: bool = True, want_perm: bool = True, threads: int = 1) -> OracleResult:
+    """Run the oracle ORB build. Inputs are copied unless copy=False (then permuted in place).
+    levels=None runs max_levels(d). threads > 1 (single rank only) bisects and partitions the
+    cells of a level in parallel, with the same results."""
     if copy:
         x, y, z = (np.array(a, dtype=np.float32, copy=True) for a in (x, y, z))
     n = x.size
-    ylev = int(d).bit_length() - 1
-    levels = ylev if levels is None else levels
+    levels = max_levels(d) if levels is None else levels
     heap = np.zeros(2 * d - 1, CELL_DTYPE)
     ranges = np.zeros((nranks, 2 * d - 1, 2), np.uint32)
     perm = np.empty(n, np.uint32) if want_perm else None
@@ -185,7 +203,7 @@ def build_tree(x, y, z, d: int, levels: int | None = None, lower=(-0.5, -0.5, -0
     rc = lib().oracle_build(_f(x), _f(y), _f(z), n, d, levels, _f(lo), _f(hi),
                             heap.ctypes.data_as(ctypes.c_void_p), _u32(ranges), _u32(perm),
                             iters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), nranks,
-                            1 if make_axis else 0, ctypes.byref(st))
+                            1 if make_axis else 0, threads, ctypes.byref(st))
     if rc != 0:
         raise ValueError(f"oracle_build rejected the arguments (code {rc})")
     stats = {

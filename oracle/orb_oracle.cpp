@@ -335,17 +335,37 @@ int64_t oracle_hoare(float *x, float *y, float *z, uint32_t *perm, uint64_t begi
                  degenerate);
 }
 
+// Cell::getNLevels() and getNCellsOnLastLevel() (src/cell.h:65-72) for nLeafCells = d:
+// depth = ceil(log2 d), last = 2d - 2^depth.
+void oracle_level_shape(uint32_t d, uint32_t *depth, uint32_t *last) {
+    uint32_t k = 0;
+    while ((1ull << k) < d) ++k;
+    *depth = k;
+    *last = (uint32_t)(2ull * d - (1ull << k));
+}
+
+// Split levels a build of d leaves may run: log2(d) for a power of two (every cell split
+// down to one leaf); otherwise the reference driver's own bound, getNLevels() - 1
+// (src/orbit.cpp:102), since its level slices name no complete level below it.
+uint32_t oracle_max_levels(uint32_t d) {
+    uint32_t depth, last;
+    oracle_level_shape(d, &depth, &last);
+    if ((d & (d - 1)) == 0) return depth;
+    return depth ? depth - 1 : 0;
+}
+
 int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t levels,
                  const float lower[3], const float upper[3], oracle_cell_t *heap,
                  uint32_t *ranges, uint32_t *perm, uint8_t *iters, int nranks, int make_axis,
-                 oracle_stats_t *stats) {
-    if (!x || !y || !z || !heap || !ranges || d == 0 || (d & (d - 1)) != 0) return -1;
+                 int threads, oracle_stats_t *stats) {
+    if (!x || !y || !z || !heap || !ranges || d == 0 || d > (1u << 30)) return -1;
     if (n >= (1ull << 31)) return -2;
-    uint32_t y_levels = 0;
-    while ((1u << y_levels) < d) ++y_levels;
-    if (levels > y_levels || levels >= ORACLE_MAX_LEVELS) return -3;
+    if (levels > oracle_max_levels(d) || levels >= ORACLE_MAX_LEVELS) return -3;
     if (nranks < 1) nranks = 1;
     if ((uint64_t)nranks > std::max<uint64_t>(n, 1)) nranks = (int)std::max<uint64_t>(n, 1);
+    if (threads < 1 || nranks > 1) threads = 1;  // cell-parallel only in single-rank mode
+    uint32_t depth, last_cells;
+    oracle_level_shape(d, &depth, &last_cells);
 
     oracle_stats_t st;
     std::memset(&st, 0, sizeof st);
@@ -382,17 +402,24 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
         rk[r].rng[1] = (uint32_t)rk[r].n;
         if (make_axis) rk[r].axis_t.resize(rk[r].n + 1);
     }
-    RankPool pool(nranks);
+    RankPool pool(std::max(nranks, threads));
 
     std::vector<uint32_t> counts, counts_left;
     std::vector<std::atomic<uint32_t>> degen(1);
     degen[0] = 0;
 
     for (uint32_t l = 1; l <= levels; ++l) {
-        // orbit.cpp:104-111 (getNCellsOnLastLevel() == d for a power-of-two d)
+        // orbit.cpp:104-111: cells [2^(l-1)-1, min(getNCellsOnLastLevel(), 2^l) - 2]. For
+        // some d that is not a power of two the slice is empty (b < a); the reference then
+        // runs its services on a non-positive cell count, which is undefined: here the
+        // level does nothing.
         const int a = (1 << (l - 1)) - 1;
-        const int b = std::min<int>((int)d, 1 << l) - 2;
+        const int b = std::min<int>((int)last_cells, 1 << l) - 2;
         const int n_cells = b - a + 1;
+        if (n_cells <= 0) {
+            st.levels_built = l;
+            continue;
+        }
         Cell *cells = heap + a;
         counts.assign(n_cells, 0);
         counts_left.assign(n_cells, 0);
@@ -400,6 +427,7 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
         if (make_axis) {  // makeAxis.cpp:16-30
             double ts = now_s();
             pool.run([&](int r) {
+                if (r >= nranks) return;
                 Rank &R = rk[r];
                 for (int c = 0; c < n_cells; ++c) {
                     const Cell &cell = cells[c];
@@ -418,53 +446,117 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
 
         // orbit.cpp:146-232
         double ts = now_s();
-        bool found_all = false;
-        int j = 0;
-        while (!found_all && j < 32) {
-            ++j;
-            found_all = true;
-            pool.run([&](int r) {  // countLeft.cpp:16-39 on every rank
-                Rank &R = rk[r];
-                R.out.assign(n_cells, 0);
-                for (int c = 0; c < n_cells; ++c) {
-                    const Cell &cell = cells[c];
-                    if (cell.foundCut) continue;
-                    uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
-                    const float *keys;
-                    if (make_axis) {
-                        keys = R.axis_t.data();
-                    } else {
-                        int ax = eff_axis(cell);
-                        keys = (ax == 0 ? x : ax == 1 ? y : z) + R.off;
-                    }
-                    R.out[c] = count_left(keys, bg, en, get_cut(cell));
-                }
-            });
-            for (int c = 0; c < n_cells; ++c) {  // Combine: elementwise sum
-                uint32_t s = 0;
-                for (int r = 0; r < nranks; ++r) s += rk[r].out[c];
-                counts_left[c] = s;
-            }
-            for (int c = 0; c < n_cells; ++c) {
+        if (threads > 1) {
+            // Single rank, cells in parallel. The loop of orbit.cpp:146-232 treats the cells of
+            // a level independently: a cell's margins, counts and its test depend on that cell
+            // alone, and the loop ends for it once it is found or at the 32nd sweep, whatever
+            // the other cells do. So every cell runs its own loop here, with the same counts,
+            // the same test and the same cap: identical cells, iterations and statistics.
+            // A level of fewer cells than threads splits each count over the threads instead
+            // (an integer sum, so the split does not change it).
+            const float *axes[3] = {x, y, z};
+            std::vector<uint32_t> jdone(n_cells, 0);
+            std::vector<uint64_t> counted(n_cells, 0);
+            auto bisect = [&](int c, auto &&count_fn) {
                 Cell &cell = cells[c];
-                if (cell.foundCut) continue;
-                ++st.cell_counts;
-                st.elements_counted += counts[c];
-                if (iters) iters[cell.id] = (uint8_t)j;
-                int dir = convergence(counts_left[c], counts[c], cell.nLeafCells, nullptr);
-                if (dir == 0) {
-                    cell.foundCut = 1;
-                } else if (dir > 0) {
-                    cell.cutMarginRight = get_cut(cell);
-                    found_all = false;
-                } else {
-                    cell.cutMarginLeft = get_cut(cell);
-                    found_all = false;
+                int j = 0;
+                while (!cell.foundCut && j < 32) {
+                    ++j;
+                    const uint32_t bg = rk[0].rng[2 * cell.id], en = rk[0].rng[2 * cell.id + 1];
+                    const uint32_t cl = count_fn(axes[eff_axis(cell)], bg, en, get_cut(cell));
+                    counted[c] += counts[c];
+                    if (iters) iters[cell.id] = (uint8_t)j;
+                    const int dir = convergence(cl, counts[c], cell.nLeafCells, nullptr);
+                    if (dir == 0)
+                        cell.foundCut = 1;
+                    else if (dir > 0)
+                        cell.cutMarginRight = get_cut(cell);
+                    else
+                        cell.cutMarginLeft = get_cut(cell);
+                }
+                jdone[c] = (uint32_t)j;
+            };
+            if (n_cells >= threads) {
+                std::atomic<int> next(0);
+                pool.run([&](int) {
+                    for (int c; (c = next.fetch_add(1)) < n_cells;)
+                        bisect(c, [](const float *k, uint32_t bg, uint32_t en, float cut) {
+                            return count_left(k, bg, en, cut);
+                        });
+                });
+            } else {
+                std::vector<uint32_t> part(threads);
+                for (int c = 0; c < n_cells; ++c)
+                    bisect(c, [&](const float *k, uint32_t bg, uint32_t en, float cut) {
+                        const uint64_t len = en - bg, chunk = (len + threads - 1) / threads;
+                        pool.run([&](int t) {
+                            const uint64_t b0 = std::min<uint64_t>(len, t * chunk);
+                            const uint64_t e0 = std::min<uint64_t>(len, b0 + chunk);
+                            part[t] = count_left(k, bg + b0, bg + e0, cut);
+                        });
+                        uint32_t s = 0;
+                        for (uint32_t v : part) s += v;
+                        return s;
+                    });
+            }
+            uint32_t jmax = 0;
+            for (int c = 0; c < n_cells; ++c) {
+                jmax = std::max(jmax, jdone[c]);
+                st.cell_counts += jdone[c];
+                st.elements_counted += counted[c];
+            }
+            // the level loop of orbit.cpp:148 runs until every cell is found or 32 sweeps
+            st.iterations[l - 1] = jmax;
+        } else {
+            bool found_all = false;
+            int j = 0;
+            while (!found_all && j < 32) {
+                ++j;
+                found_all = true;
+                pool.run([&](int r) {  // countLeft.cpp:16-39 on every rank
+                    if (r >= nranks) return;
+                    Rank &R = rk[r];
+                    R.out.assign(n_cells, 0);
+                    for (int c = 0; c < n_cells; ++c) {
+                        const Cell &cell = cells[c];
+                        if (cell.foundCut) continue;
+                        uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
+                        const float *keys;
+                        if (make_axis) {
+                            keys = R.axis_t.data();
+                        } else {
+                            int ax = eff_axis(cell);
+                            keys = (ax == 0 ? x : ax == 1 ? y : z) + R.off;
+                        }
+                        R.out[c] = count_left(keys, bg, en, get_cut(cell));
+                    }
+                });
+                for (int c = 0; c < n_cells; ++c) {  // Combine: elementwise sum
+                    uint32_t s = 0;
+                    for (int r = 0; r < nranks; ++r) s += rk[r].out[c];
+                    counts_left[c] = s;
+                }
+                for (int c = 0; c < n_cells; ++c) {
+                    Cell &cell = cells[c];
+                    if (cell.foundCut) continue;
+                    ++st.cell_counts;
+                    st.elements_counted += counts[c];
+                    if (iters) iters[cell.id] = (uint8_t)j;
+                    int dir = convergence(counts_left[c], counts[c], cell.nLeafCells, nullptr);
+                    if (dir == 0) {
+                        cell.foundCut = 1;
+                    } else if (dir > 0) {
+                        cell.cutMarginRight = get_cut(cell);
+                        found_all = false;
+                    } else {
+                        cell.cutMarginLeft = get_cut(cell);
+                        found_all = false;
+                    }
                 }
             }
+            st.iterations[l - 1] = (uint32_t)j;
         }
         st.t_count_s += now_s() - ts;
-        st.iterations[l - 1] = (uint32_t)j;
         for (int c = 0; c < n_cells; ++c)
             if (!cells[c].foundCut) ++st.unfound_cells;
 
@@ -476,26 +568,36 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
             heap[rc.id] = rc;
         }
 
-        // partition.cpp:18-62 on every rank
+        // partition.cpp:18-62 on every rank (single rank with threads: cells in parallel,
+        // their ranges are disjoint)
         ts = now_s();
-        pool.run([&](int r) {
-            Rank &R = rk[r];
-            uint32_t local_degen = 0;
-            for (int c = 0; c < n_cells; ++c) {
-                const Cell &cell = cells[c];
-                uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
-                int dg = 0;
-                int64_t i = hoare(x + R.off, y + R.off, z + R.off, perm ? perm + R.off : nullptr,
-                                  bg, en, eff_axis(cell), get_cut(cell), true, &dg);
-                local_degen += (uint32_t)dg;
-                const int lcid = 2 * cell.id + 1, rcid = 2 * cell.id + 2;
-                R.rng[2 * lcid] = bg;
-                R.rng[2 * lcid + 1] = (uint32_t)i;
-                R.rng[2 * rcid] = (uint32_t)i;
-                R.rng[2 * rcid + 1] = en;
-            }
-            degen[0] += local_degen;
-        });
+        auto part_cell = [&](Rank &R, const Cell &cell) -> uint32_t {
+            uint32_t bg = R.rng[2 * cell.id], en = R.rng[2 * cell.id + 1];
+            int dg = 0;
+            int64_t i = hoare(x + R.off, y + R.off, z + R.off, perm ? perm + R.off : nullptr, bg, en,
+                              eff_axis(cell), get_cut(cell), true, &dg);
+            const int lcid = 2 * cell.id + 1, rcid = 2 * cell.id + 2;
+            R.rng[2 * lcid] = bg;
+            R.rng[2 * lcid + 1] = (uint32_t)i;
+            R.rng[2 * rcid] = (uint32_t)i;
+            R.rng[2 * rcid + 1] = en;
+            return (uint32_t)dg;
+        };
+        if (threads > 1) {
+            std::atomic<int> next(0);
+            pool.run([&](int) {
+                uint32_t local_degen = 0;
+                for (int c; (c = next.fetch_add(1)) < n_cells;) local_degen += part_cell(rk[0], cells[c]);
+                degen[0] += local_degen;
+            });
+        } else {
+            pool.run([&](int r) {
+                if (r >= nranks) return;
+                uint32_t local_degen = 0;
+                for (int c = 0; c < n_cells; ++c) local_degen += part_cell(rk[r], cells[c]);
+                degen[0] += local_degen;
+            });
+        }
         st.t_partition_s += now_s() - ts;
         st.levels_built = l;
     }

@@ -85,9 +85,13 @@ int64_t oracle_hoare(float *x, float *y, float *z, uint32_t *perm, uint64_t begi
 /*
  * Full ORB build, in place on x,y,z (the particle order after the build is the
  * reference's partitioned order).
- *   d        leaf cells, a power of two; heap holds 2d-1 cells, ranges 2*(2d-1) uint32
- *   levels   split levels to run: log2(d) gives d leaves, log2(d)-1 is the reference's
- *            own loop bound (src/orbit.cpp:102)
+ *   d        leaf cells (1 .. 2^30); heap holds 2d-1 cells, ranges 2*(2d-1) uint32
+ *   levels   split levels to run, at most oracle_max_levels(d). Level l takes the heap cells
+ *            [2^(l-1)-1, min(getNCellsOnLastLevel(), 2^l) - 2] (src/orbit.cpp:104-107); for
+ *            a power of two that is every cell of the level, log2(d) levels give d leaves
+ *            and log2(d)-1 is the reference's own loop bound (src/orbit.cpp:102). For any
+ *            other d the reference's bound getNLevels()-1 is the most; a slice that comes out
+ *            empty (b < a) is a level without cells.
  *   perm     optional: original index of the particle at each position
  *   iters    optional: bisection iterations spent on each heap cell
  *   nranks   1 = canonical single-rank oracle. >1 = the reference's MDL semantics: the
@@ -96,12 +100,23 @@ int64_t oracle_hoare(float *x, float *y, float *z, uint32_t *perm, uint64_t begi
  *            `ranges` then holds nranks consecutive range maps.
  *   make_axis  1 = also perform the per-level cut-axis gather the reference performs
  *            (src/services/makeAxis.cpp); results are identical, only timing changes.
+ *   threads  single-rank mode only: the cells of a level are bisected and partitioned on
+ *            this many threads (each cell runs its own loop of src/orbit.cpp:146-232, which
+ *            depends on that cell alone), and a level of fewer cells splits each count over
+ *            the threads. Results and statistics are those of threads = 1.
  * Returns 0 on success, a negative value on invalid arguments.
  */
 int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t levels,
                  const float lower[3], const float upper[3], oracle_cell_t *heap,
                  uint32_t *ranges, uint32_t *perm, uint8_t *iters, int nranks,
-                 int make_axis, oracle_stats_t *stats);
+                 int make_axis, int threads, oracle_stats_t *stats);
+
+/* Cell::getNLevels() (depth = ceil(log2 d)) and getNCellsOnLastLevel() (2d - 2^depth) of
+ * src/cell.h:65-72. */
+void oracle_level_shape(uint32_t d, uint32_t *depth, uint32_t *last);
+/* Most split levels of a build of d leaves: log2(d) for a power of two, else the
+ * reference's bound getNLevels() - 1. */
+uint32_t oracle_max_levels(uint32_t d);
 
 #ifdef __cplusplus
 }

@@ -80,3 +80,12 @@ def test_batch_rejects_overlap(ctx, engine):
     inst = [{"offset": 0, "n": 60, "d": 4}, {"offset": 50, "n": 50, "d": 4}]
     with pytest.raises(engine.OrbError):
         ctx.build_batch(x, x.copy(), x.copy(), inst)
+
+
+def test_batch_non_power_of_two_instances(ctx, oracle):
+    """Instances with leaf counts that are not powers of two, beside powers of two, at
+    their default (most) levels and below."""
+    specs = [("uniform", 41, 20000, 3, 0), ("plummer", 42, 30000, 100, 0),
+             ("uniform", 43, 15000, 64, 0), ("plummer", 44, 40000, 1000, 0),
+             ("uniform", 45, 9000, 12, 2), ("uniform", 46, 25000, 7, 0)]
+    check_batch(ctx, oracle, specs, gap=5)

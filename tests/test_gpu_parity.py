@@ -5,7 +5,6 @@ range map, the permutation (particle -> position) and the reordered coordinates.
 import numpy as np
 import pytest
 
-from helpers import tree_properties
 
 pytestmark = pytest.mark.gpu
 
@@ -186,19 +185,28 @@ def test_large_parity(ctx, oracle):
     run_both(ctx, oracle, x, y, z, 1 << 13)
 
 
-def test_headline_properties(ctx, oracle, engine):
-    """2^27 particles, 2^16 leaves: size-independent properties of the device build."""
-    n, d = 1 << 27, 1 << 16
-    x, y, z = ctx.generate_host(engine.ORB_GEN_UNIFORM, 2027, n)
-    res = ctx.build(x, y, z, d)
-    tree_properties(x, y, z, res.heap, res.ranges, n, d, 16)
-    perm = res.perm
-    seen = np.zeros(n, np.bool_)
-    seen[perm] = True
-    assert seen.all()
-    leaves = res.ranges[(1 << 16) - 1:]
-    sizes = leaves[:, 1].astype(np.int64) - leaves[:, 0]
-    assert sizes.min() >= 2048 - 64 and sizes.max() <= 2048 + 64
+@pytest.mark.parametrize("d", [3, 5, 6, 7, 11, 12, 100, 1000])
+def test_non_power_of_two_leaves(any_ctx, oracle, d):
+    """d not a power of two, at the reference's own bound getNLevels()-1: the level slices
+    of src/orbit.cpp:104-107 (partial or empty where getNCellsOnLastLevel() cuts them), the
+    ceil(k/2) split of src/cell.h:79 and the ratio ceil(k/2)/k of src/orbit.cpp:204, which
+    rounds in float32 for odd k (2/3 for k = 3)."""
+    n = 1 << 16
+    x, y, z = (oracle.gen_uniform if d % 2 else oracle.gen_plummer)(300 + d, n)
+    res, ref = run_both(any_ctx, oracle, x, y, z, d)
+    assert res.info["levels_built"] == oracle.max_levels(d)
+    # the odd leaf counts really occur (not only at d itself)
+    split = ref.heap[ref.heap["nLeafCells"] > 0]
+    if d in (3, 7, 11, 100, 1000):
+        assert (split["nLeafCells"] % 2 == 1).any()
+
+
+def test_non_power_of_two_lower_levels_and_bounds(ctx, engine, oracle):
+    x, y, z = oracle.gen_uniform(333, 50000)
+    for d, levels in ((100, 3), (1000, 5), (6, 1)):
+        run_both(ctx, oracle, x, y, z, d, levels=levels)
+    with pytest.raises(engine.OrbError):
+        ctx.build(x.copy(), y.copy(), z.copy(), 100, levels=7)  # beyond getNLevels()-1
 
 
 @pytest.mark.parametrize("kind,seed,logn,logd", [("plummer", 501, 20, 15), ("uniform", 502, 21, 12),

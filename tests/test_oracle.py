@@ -317,4 +317,98 @@ def test_edge_cases(oracle):
     r = oracle.build_tree(xo, xo.copy(), xo.copy(), 4, lower=lo, upper=hi)
     assert r.stats["levels_built"] == 2
     with pytest.raises(ValueError):
-        oracle.build_tree(x, x, x, 3)  # not a power of two
+        oracle.build_tree(x, x, x, 0)  # no leaves
+    with pytest.raises(ValueError):
+        oracle.build_tree(x, x, x, 100, levels=7)  # beyond the reference's bound for d=100
+
+
+def _grid(seed, n, values=32):
+    rng = np.random.default_rng(seed)
+    return [(rng.integers(0, values, n).astype(np.float32) / np.float32(values) - np.float32(0.5))
+            for _ in range(3)]
+
+
+@pytest.mark.parametrize("kind,n,d", [("uniform", 1 << 16, 1 << 8), ("plummer", 1 << 17, 1 << 10),
+                                      ("grid", 1 << 15, 1 << 7), ("uniform", 100000, 100),
+                                      ("plummer", 50000, 6), ("grid", 5000, 12), ("uniform", 3, 4)])
+def test_threads_give_the_single_thread_tree(oracle, kind, n, d):
+    """Cells bisected and partitioned in parallel (and single cells counted in chunks) give
+    the single-thread oracle's heap, ranges, order, iterations and statistics."""
+    if kind == "grid":
+        x, y, z = _grid(n, n)
+    else:
+        x, y, z = (oracle.gen_uniform if kind == "uniform" else oracle.gen_plummer)(n % 97, n)
+    a = oracle.build_tree(x, y, z, d)
+    b = oracle.build_tree(x, y, z, d, threads=8)
+    assert a.heap.tobytes() == b.heap.tobytes()
+    assert np.array_equal(a.ranges, b.ranges) and np.array_equal(a.perm, b.perm)
+    assert np.array_equal(a.iters, b.iters) and np.array_equal(a.x, b.x)
+    strip = lambda st: {k: v for k, v in st.items() if not k.startswith("t_")}
+    assert strip(a.stats) == strip(b.stats)
+
+
+def test_non_power_of_two_slices(oracle):
+    """d not a power of two follows the reference's own level loop (src/orbit.cpp:102-107):
+    levels up to getNLevels()-1, heap slices cut by getNCellsOnLastLevel() (partial or
+    empty), ceil(k/2) leaves to the left child (src/cell.h:79)."""
+    assert [oracle.level_shape(d) for d in (1, 2, 3, 5, 6, 9, 11, 100, 1000)] == \
+        [(0, 1), (1, 2), (2, 2), (3, 2), (3, 4), (4, 2), (4, 6), (7, 72), (10, 976)]
+    assert [oracle.max_levels(d) for d in (1, 2, 3, 5, 6, 8, 9, 100, 1024)] == \
+        [0, 1, 1, 2, 2, 3, 3, 6, 10]
+    x, y, z = oracle.gen_uniform(4, 20000)
+    # d = 11: level 3 holds cells 3 and 4 only (min(6, 8) - 2 = 4): cells 5 and 6 stay leaves
+    r = oracle.build_tree(x, y, z, 11)
+    assert list(r.heap["nLeafCells"][:7]) == [11, 6, 5, 3, 3, 3, 2]
+    assert list(r.heap["nLeafCells"][7:11]) == [2, 1, 2, 1] and np.all(r.heap["nLeafCells"][11:] == 0)
+    assert r.stats["levels_built"] == 3
+    # d = 9: level 2 is empty (min(2, 4) - 2 = 0 < 1): only the root is split
+    r = oracle.build_tree(x, y, z, 9)
+    assert list(r.heap["nLeafCells"][:3]) == [9, 5, 4] and np.all(r.heap["nLeafCells"][3:] == 0)
+    # d = 3: the root splits 2 + 1 with the float ratio 2/3 (0.6666667f) in its test
+    r = oracle.build_tree(x, y, z, 3)
+    b, e = r.ranges[0][1]
+    assert abs(int(e - b) - 20000 * 2 / 3) < 3
+    assert oracle.convergence(13333, 20000, 3) == (0, 0)
+
+
+LEAF_RATIO_DRIVER = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include "orb_leaf_ratio.h"
+int main() {
+    unsigned long long bad = 0, cnt = 0, s = 12345;
+    auto chk = [&](int32_t n) {
+        float r = (float)(std::ceil(n / 2.0) / n);   // src/orbit.cpp:204
+        float q = orb::leaf_ratio(n);
+        uint32_t a, b; std::memcpy(&a, &r, 4); std::memcpy(&b, &q, 4);
+        ++cnt; if (a != b) ++bad;
+    };
+    for (int32_t n = 1; n < (1 << 22); ++n) chk(n);
+    for (int i = 0; i < 4000000; ++i) {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        chk((int32_t)((s >> 33) % (1u << 30)) + 1);
+    }
+    for (int32_t n = (1 << 30) - 50000; n <= (1 << 30); ++n) chk(n);
+    std::printf("%llu %llu\n", cnt, bad);
+    return bad != 0;
+}
+"""
+
+
+def test_engine_leaf_ratio_is_the_references(tmp_path):
+    """The engine's integer evaluation of float(ceil(k/2.0)/k) (a double quotient rounded to
+    float) equals the reference's double expression for every k below 2^22, 4M random k up
+    to 2^30 and the top 50001."""
+    import subprocess
+    src = tmp_path / "ratio.cpp"
+    src.write_text(LEAF_RATIO_DRIVER)
+    exe = tmp_path / "ratio"
+    inc = os.path.join(os.path.dirname(GOLDEN), "..", "gpu-load-balance_gb300", "csrc")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", inc, "-o", str(exe),
+                    str(src)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    cnt, bad = (int(v) for v in out.stdout.split())
+    assert bad == 0 and cnt > 8_000_000

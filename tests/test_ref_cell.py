@@ -90,9 +90,31 @@ def test_splits_are_the_references(ref, oracle, kind, seed, n, d):
     assert checked >= d // 2
 
 
-def test_level_slices_are_the_references(ref):
-    for y in range(0, 20):
-        d = 1 << y
+def test_level_slices_are_the_references(ref, oracle):
+    ds = [1 << y for y in range(0, 21)] + list(range(1, 1100)) + [12345, 99999, (1 << 20) + 3]
+    for d in ds:
         nl, nc = ctypes.c_int(), ctypes.c_int()
         ref.ref_levels(d, ctypes.byref(nl), ctypes.byref(nc))
-        assert (nl.value, nc.value) == (y, d)
+        assert (nl.value, nc.value) == oracle.level_shape(d), d
+        if d & (d - 1) == 0:
+            assert (nl.value, nc.value) == (d.bit_length() - 1, d)
+
+
+@pytest.mark.parametrize("d", [3, 6, 7, 11, 12, 100, 1000])
+def test_non_power_of_two_splits_are_the_references(ref, oracle, d):
+    """Trees of d leaves not a power of two: every split (leaf counts ceil(k/2) and the rest,
+    boxes, axes, margins) is the reference's cut() + setCutAxis() + setCutMargin()."""
+    x, y, z = oracle.gen_plummer(d, 1 << 14)
+    heap = oracle.build_tree(x, y, z, d).heap
+    checked = 0
+    for cid in range(len(heap)):
+        if heap[cid]["nLeafCells"] == 0 or 2 * cid + 2 >= len(heap) or heap[2 * cid + 1]["nLeafCells"] == 0:
+            continue
+        parent = heap[cid:cid + 1].copy()
+        left, right = np.zeros(1, heap.dtype), np.zeros(1, heap.dtype)
+        ref.ref_split(parent.ctypes.data, left.ctypes.data, right.ctypes.data)
+        for child, want in ((left, heap[2 * cid + 1]), (right, heap[2 * cid + 2])):
+            for f in ("id", "nLeafCells", "prevCutAxis", "cutAxis", "lower", "upper"):
+                assert np.array_equal(child[0][f], want[f]), f"d={d} cell {cid}: {f}"
+        checked += 1
+    assert checked >= 1
