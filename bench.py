@@ -7,15 +7,22 @@ by a device-to-device restore of the unpartitioned input (the build partitions i
   value      particles/s with inputs resident in HBM (restore + build per step)
   e2e        particles/s through orb_build with pinned HOST buffers, as the reference's
              driver calls it: H2D of x,y,z, build, D2H of the reordered x,y,z, the cell heap
-             and the range map (the reference has no permutation output)
-  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time (live, on the
-             engine's stream) against the measured HBM copy bandwidth
+             and the range map (the reference has no permutation output); beside it the
+             host link's own copy rate measured in the same run (its ceiling)
+  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time in the timed
+             region (on the engine's stream) against the measured HBM copy bandwidth
+  count_left every count-left launch of the timed region (same events), against the same peak
   cpu_baseline  the CPU oracle with the reference's MDL semantics (one rank per host core,
-             per-cell counts summed, per-rank Hoare partition) on the same workload
+             per-cell counts summed, per-rank Hoare partition) on a bounded sample; the same
+             leg runs the single-rank oracle on the benchmark's own inputs (outside every
+             timed region) as the checker of the GPU outputs: "parity"
+  clustered  the same measurements for 2^26 Plummer-clustered particles into 2^18 leaves
+  batched    128 uneven instances in one batched build against one build at a time
+  served     a Poisson request stream through the continuous-batching server
 
---impl reference times that CPU implementation alone (rank 0), as the reference arm.
-With torchrun (N>1) every rank builds its own replica on its own GPU (the path has no
-data exchange on one GPU per box): value sums the particles of all ranks.
+--impl reference times the CPU implementation alone (rank 0), as the reference arm, with
+the same config. With torchrun (N>1) every rank builds its own replica on its own GPU (the
+path has no data exchange on one GPU per box): value sums the particles of all ranks.
 """
 from __future__ import annotations
 
@@ -39,8 +46,28 @@ SEED = 20270
 METRIC = "orb_build_particles_per_s"
 WARM_WIDTH = 8.0  # warm rebuild: bracket factor (half-width = factor x extent / sqrt(n))
 UNIT = "particles/s"
-WORKLOAD = "plain ORB, 2^27 uniform float32 particles in [-0.5,0.5)^3, 2^16 leaf cells"
 FALLBACK_HBM_GBS = 6800.0
+CLUSTERED = (1 << 26, 1 << 18)
+TRAFFIC_PROFILE = "dram_traffic_part_swap_hist_classify_subtree_2p24_2p13.txt"
+# every kernel kind that counts keys below a cut (the count-left family)
+COUNT_LEFT_KERNELS = ("count_left_hist", "bisect_tile", "bisect_cta", "count_left_sample",
+                      "count_left_sample_pick")
+PARTITION_KERNELS = ("part_classify", "part_scan", "part_cells", "part_swap", "part_finish")
+
+
+def workload_name(kind: str, n: int, d: int) -> str:
+    lg = lambda v: f"2^{v.bit_length() - 1}" if v & (v - 1) == 0 else str(v)
+    what = "uniform float32 particles in [-0.5,0.5)^3" if kind == "uniform" else \
+        "float32 particles, 90% from 64 Plummer spheres + 10% uniform, in [-0.5,0.5)^3"
+    return f"plain ORB, {lg(n)} {what}, {lg(d)} leaf cells"
+
+
+def workload_config(n: int, d: int, world: int) -> dict:
+    """The `config` both arms print (the driver compares them)."""
+    return {"workload": workload_name("uniform", n, d), "particles": n, "leaves": d,
+            "levels": d.bit_length() - 1, "parallelism": f"replicas x{world}",
+            "l2": "inputs 1.5 GB > 129 MB L2 (no flush needed)" if 12 * n > (129 << 20)
+            else "inputs smaller than the 129 MB L2"}
 
 
 def dist_env():
@@ -80,7 +107,6 @@ class ClockSampler:
         except Exception:
             self.proc = None
             return
-        self.mark = None
         self.t = threading.Thread(target=self._read, daemon=True)
         self.t.start()
 
@@ -129,7 +155,7 @@ def traffic_ratio(kernel: str):
     with the units a launch processes)."""
     names = {"part_swap": "k_part_swap", "count_left_hist": "k_hist", "part_classify": "k_part_classify",
              "bisect_tile": "k_bisect_tile", "subtree": "k_subtree"}
-    path = os.path.join(ROOT, "profiles", "dram_traffic_part_swap_hist_classify_subtree_2p24_2p13.txt")
+    path = os.path.join(ROOT, "profiles", TRAFFIC_PROFILE)
     try:
         with open(path) as f:
             for line in f:
@@ -151,22 +177,26 @@ def gpu_id_for(local_rank: int):
 
 
 # ------------------------------------------------------------------------------------------
-# CPU implementation (the oracle with the reference's MDL semantics)
+# CPU leg: the oracle as the timed CPU baseline (MDL semantics) and as the checker
 # ------------------------------------------------------------------------------------------
-def cpu_build_probe(n: int, d: int, threads: int):
+def _oracle():
     sys.path.insert(0, ORACLE_DIR)
-    import oracle as O  # the checker; used here only as the timed CPU baseline
+    import oracle as O  # the checker and the CPU baseline; never on the GPU path
     O.build()
+    return O
+
+
+def cpu_build_probe(n: int, d: int, threads: int):
+    O = _oracle()
     x, y, z = O.gen_uniform(SEED, n, nthreads=threads)
     t = time.perf_counter()
     r = O.build_tree(x, y, z, d, nranks=threads, make_axis=True, copy=False, want_perm=False)
     return time.perf_counter() - t, r.stats
 
 
-def cpu_sample_size(budget_s: float, steps: int, threads: int):
+def cpu_sample_size(n: int, d: int, budget_s: float, steps: int, threads: int):
     """Largest (n, d) with the workload's particles-per-leaf whose run fits the budget."""
-    n, d = N_PARTICLES, LEAVES
-    t_probe, _ = cpu_build_probe(n >> 5, d >> 5, threads)
+    t_probe, _ = cpu_build_probe(max(n >> 5, 1 << 12), max(d >> 5, 2), threads)
     per_step = t_probe * 32 * 1.15  # levels grow by 5 at full size
     while per_step * steps > budget_s and n > (1 << 20):
         n >>= 1
@@ -175,9 +205,9 @@ def cpu_sample_size(budget_s: float, steps: int, threads: int):
     return n, d
 
 
-def run_cpu(steps: int, warmup: int, budget_s: float):
+def run_cpu(n_full: int, d_full: int, steps: int, warmup: int, budget_s: float):
     threads = os.cpu_count() or 1
-    n, d = cpu_sample_size(budget_s, steps + warmup, threads)
+    n, d = cpu_sample_size(n_full, d_full, budget_s, steps + warmup, threads)
     times = []
     stats = None
     for i in range(warmup + steps):
@@ -194,24 +224,288 @@ def run_cpu(steps: int, warmup: int, budget_s: float):
             ("t_make_axis_s", "t_count_s", "t_partition_s", "t_total_s")}}
 
 
+def check_parity(job):
+    """The checker: the single-rank oracle (src/orbit.cpp:102-275 restated, cells in
+    parallel) on the job's own inputs, compared bit for bit with the GPU's outputs."""
+    import numpy as np
+    O = _oracle()
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    out = {"oracle": "single-rank restatement of the reference's CPU path, run on the "
+                     "benchmark's own inputs", "compared": ["heap", "ranges", "perm", "x", "y", "z"]}
+    ok, cells, particles = True, 0, 0
+    for inst in job["instances"]:
+        x, y, z = (job["x"][inst["offset"]:inst["offset"] + inst["n"]],
+                   job["y"][inst["offset"]:inst["offset"] + inst["n"]],
+                   job["z"][inst["offset"]:inst["offset"] + inst["n"]])
+        ref = O.build_tree(x, y, z, inst["d"], threads=threads)
+        heap, ranges, gx, gy, gz, perm = inst["gpu"]
+        same = (heap.tobytes() == ref.heap.tobytes() and np.array_equal(ranges, ref.ranges[0])
+                and np.array_equal(perm, ref.perm)
+                and all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                        for a, b in ((gx, ref.x), (gy, ref.y), (gz, ref.z))))
+        ok = ok and same
+        cells += len(ref.heap)
+        particles += inst["n"]
+    out.update({"bit_exact": bool(ok), "instances": len(job["instances"]), "cells": cells,
+                "particles": particles, "oracle_s": round(time.perf_counter() - t, 2)})
+    return out
+
+
 def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    cpu = run_cpu(args.steps, args.warmup, budget_s=150.0)
+    cpu = run_cpu(args.particles, args.leaves, args.steps, args.warmup, budget_s=150.0)
     line = {
         "impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": cpu["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform)",
-        "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "leaves": LEAVES,
-                   "l2": "inputs 1.5 GB > L2"},
+        "config": workload_config(args.particles, args.leaves, world),
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ------------------------------------------------------------------------------------------
+# One plain workload (headline or clustered): device-resident steps, per-kernel profile,
+# roofline, count-left, e2e through pinned host buffers, GPU outputs for the checker
+# ------------------------------------------------------------------------------------------
+def measure_link(torch, dev, nbytes: int, reps: int = 3):
+    """The host link's copy rate with one plain copy of nbytes each way (pinned host)."""
+    h = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+    dbuf = torch.empty(nbytes // 4, dtype=torch.float32, device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    dbuf.copy_(h, non_blocking=True)
+    h.copy_(dbuf, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    ev[0].record()
+    for _ in range(reps):
+        dbuf.copy_(h, non_blocking=True)
+    ev[1].record()
+    for _ in range(reps):
+        h.copy_(dbuf, non_blocking=True)
+    ev[2].record()
+    torch.cuda.synchronize(dev)
+    h2d = reps * nbytes / (ev[0].elapsed_time(ev[1]) / 1e3) / 1e9
+    d2h = reps * nbytes / (ev[1].elapsed_time(ev[2]) / 1e3) / 1e9
+    del h, dbuf
+    return h2d, d2h
+
+
+def run_plain(ctx, E, torch, dev, args, kind: str, n: int, d: int, seed: int, peak: float,
+              peak_kind: str, tuning_arg, clocks_cb=None, with_warm=False):
+    import numpy as np
+
+    gen = E.ORB_GEN_UNIFORM if kind == "uniform" else E.ORB_GEN_PLUMMER
+    x0, y0, z0 = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    ctx.generate(gen, seed, n, x0, y0, z0, device_pointers=True)
+    x, y, z = (torch.empty_like(x0) for _ in range(3))
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+    # cell heap and range map land in pinned host buffers (the API's host outputs)
+    heap_pin = torch.empty((2 * d - 1) * 52, dtype=torch.uint8, pin_memory=True)
+    ranges_pin = torch.empty((2 * d - 1) * 2, dtype=torch.int32, pin_memory=True)
+    heap_np = heap_pin.numpy().view(E.CELL_DTYPE)
+    ranges_np = ranges_pin.numpy().view(np.uint32).reshape(-1, 2)
+
+    def step(with_perm=False):
+        # the reference's outputs: reordered x,y,z, cell heap, range map (it has no
+        # permutation output; with_perm adds the engine's optional one)
+        x.copy_(x0)
+        y.copy_(y0)
+        z.copy_(z0)
+        torch.cuda.synchronize(dev)
+        return ctx.build(x, y, z, d, perm=perm if with_perm else None, device_pointers=True,
+                         heap_out=heap_np, ranges_out=ranges_np)
+
+    # launch parameters from the engine's autotuner on this workload (before any timing; the
+    # inputs are copied, every candidate's tree is checked equal)
+    t0 = time.perf_counter()
+    if tuning_arg:
+        names = ("hist_blocks_per_sm", "part_blocks_per_sm", "tile_blocks_per_sm",
+                 "sparse_keys_per_tile", "cta_min_cells", "subtree_levels", "predict_sigmas")
+        ctx.set_tuning(**dict(zip(names, (int(v) for v in tuning_arg.split(",")))))
+        tuning, tuned_by = ctx.get_tuning(), "--tuning"
+    else:
+        tuning, _ = ctx.autotune_batch(x0, y0, z0, [{"offset": 0, "n": n, "d": d}], reps=2,
+                                       device_pointers=True)
+        tuned_by = "orb_autotune_batch"
+    tune_s = time.perf_counter() - t0
+
+    # warm-up steps time every kernel: per-kernel breakdown and the dominant kernel
+    ctx.profile_reset(timing=True)
+    for _ in range(args.warmup):
+        step()
+    warm = ctx.profile()
+    warm_timed = {k: v for k, v in warm.items() if v["total_ms"] > 0}
+    dom = max(warm_timed, key=lambda k: warm_timed[k]["total_ms"])
+    # timed steps: CUDA events only around the dominant kernel's and the count-left kernels'
+    # launches (one untimed step first, so the build's CUDA graph is captured outside the
+    # timed region)
+    timed_kinds = sorted({dom, *[k for k in COUNT_LEFT_KERNELS if k in warm]})
+    ctx.profile_reset(timing=timed_kinds)
+    step()
+    ctx.profile_reset(timing=timed_kinds)
+    torch.cuda.synchronize(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if clocks_cb:
+        clocks_cb("start")
+    ev0.record()
+    infos = []
+    for _ in range(args.steps):
+        infos.append(step().info)
+    ev1.record()
+    torch.cuda.synchronize(dev)
+    if clocks_cb:
+        clocks_cb("end")
+    ms_total = ev0.elapsed_time(ev1)
+    prof = ctx.profile()
+    launches = sum(v["launches"] for v in prof.values())
+
+    # roofline of the dominant kernel (its events in the timed region)
+    dk = prof[dom]
+    achieved = dk["bytes"] / (dk["total_ms"] / 1e3) / 1e9
+    kern_ms_total = sum(v["total_ms"] for v in warm_timed.values())
+    ratio = traffic_ratio(dom)
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+        "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+        "traffic": (ratio * dk["bytes"] / dk["launches"]) if ratio else None,
+        "traffic_source": "ncu dram bytes per algorithmic byte, 2^24/2^13 capture scaled per unit"
+                          if ratio else None,
+        "dram_gbs_equivalent": round(achieved * ratio, 1) if ratio else None,
+        "bytes_per_launch": dk["bytes"] / dk["launches"],
+        "ms_per_launch": dk["total_ms"] / dk["launches"],
+        "share_of_kernel_time": round(warm_timed[dom]["total_ms"] / kern_ms_total, 4),
+    }
+    if dom == "part_swap":
+        # the partition's 36 B per particle and level model (key 4 B + coordinates 12 B read +
+        # 12 B written + index 4+4 B of an out-of-place scatter) over the levels this kernel
+        # partitions, beside the swap's own 48 B per swapped pair
+        lv = dk["launches"] / args.steps
+        model = 36.0 * n * lv * args.steps / (dk["total_ms"] / 1e3) / 1e9
+        roofline["algorithmic_bytes"] = "48 B per swapped pair (x,y,z of both read and written)"
+        roofline["model_36BN"] = {"achieved": round(model, 1), "frac": round(model / peak, 4),
+                                  "levels": lv, "bytes_per_level": 36 * n,
+                                  "note": "36 B x particles per level over the swap's event time"}
+    # count-left: every count-left launch of the timed region
+    cl_names = [k for k in COUNT_LEFT_KERNELS if k in prof and prof[k]["total_ms"] > 0]
+    cl_bytes = sum(prof[k]["bytes"] for k in cl_names) / args.steps
+    cl_ms = sum(prof[k]["total_ms"] for k in cl_names) / args.steps
+    cl_gbs = cl_bytes / (cl_ms / 1e3) / 1e9 if cl_ms else None
+    count_left = {"kernels": cl_names, "bytes_per_step": cl_bytes, "ms_per_step": round(cl_ms, 4),
+                  "achieved": round(cl_gbs, 1) if cl_gbs else None, "peak": peak, "unit": "GB/s",
+                  "frac": round(cl_gbs / peak, 4) if cl_gbs else None,
+                  "peak_source": f"{peak_kind} hbm_gbs", "timed": "CUDA events in the timed region",
+                  "bytes": "4 B per key read + 4 B per key compacted (algorithmic, engine counters)",
+                  "excluded": "the bisection inside k_subtree (the last levels' bisection and "
+                              "partition run fused in one kernel, timed as `subtree`)"
+                              if "subtree" in warm else None}
+    wsteps = max(args.warmup, 1)
+    kernels = {k: {"launches": v["launches"] // wsteps, "ms": round(v["total_ms"] / wsteps, 4),
+                   "GBps": round(v["bytes"] / (v["total_ms"] / 1e3) / 1e9, 1) if v["total_ms"] else None}
+               for k, v in warm.items()}
+    part_ms = sum(warm[k]["total_ms"] for k in PARTITION_KERNELS if k in warm) / wsteps
+
+    # the same step with the optional permutation output (one more array moved per swap); its
+    # outputs are the checker's GPU side
+    ctx.profile_reset(timing=False)
+    step(with_perm=True)
+    torch.cuda.synchronize(dev)
+    ev0.record()
+    for _ in range(args.steps):
+        res = step(with_perm=True)
+    ev1.record()
+    torch.cuda.synchronize(dev)
+    perm_ms_step = ev0.elapsed_time(ev1) / args.steps
+    gpu_out = (heap_np.copy(), ranges_np.copy(), x.cpu().numpy(), y.cpu().numpy(), z.cpu().numpy(),
+               perm.cpu().numpy().view(np.uint32))
+    inputs = (x0.cpu().numpy(), y0.cpu().numpy(), z0.cpu().numpy())
+
+    warm_rb = None
+    if with_warm:
+        # warm-started rebuild (labelled mode, not bit-identical with a cold build): the same
+        # particles displaced by sigma = 1e-3 (seeded, clamped to the box), rebuilt cold and
+        # from the previous tree's cuts
+        prev_heap = gpu_out[0]
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed + 11)
+        hi = float(np.nextafter(np.float32(0.5), np.float32(0)))
+        xd, yd, zd = ((a + 1e-3 * torch.randn(n, generator=g, device=dev)).clamp_(-0.5, hi)
+                      for a in (x0, y0, z0))
+        cold_ms, warm_ms, winfo = [], [], None
+        for i in range(args.warmup + args.steps):
+            for dst, src in ((x, xd), (y, yd), (z, zd)):
+                dst.copy_(src)
+            c = ctx.build(x, y, z, d, perm=None, device_pointers=True)
+            for dst, src in ((x, xd), (y, yd), (z, zd)):
+                dst.copy_(src)
+            w = ctx.build_warm(x, y, z, d, prev_heap, WARM_WIDTH, perm=None, device_pointers=True)
+            if i >= args.warmup:
+                cold_ms.append(c.info["device_ms"])
+                warm_ms.append(w.info["device_ms"])
+                winfo = w.info
+        del xd, yd, zd
+        warm_rb = {"workload": f"{workload_name(kind, n, d)}, particles displaced by N(0, 1e-3^2) "
+                               "per coordinate",
+                   "width": WARM_WIDTH, "cold_build_ms": round(statistics.median(cold_ms), 3),
+                   "warm_build_ms": round(statistics.median(warm_ms), 3),
+                   "speedup": round(statistics.median(cold_ms) / statistics.median(warm_ms), 3),
+                   "warm_cells": winfo["warm_cells"], "warm_resets": winfo["warm_resets"],
+                   "note": "labelled mode: a valid ORB tree, not bit-identical with the cold build"}
+
+    # end to end through the C ABI with pinned host buffers (copies inside the timed region)
+    hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
+    for h, src in ((hx, inputs[0]), (hy, inputs[1]), (hz, inputs[2])):
+        h.numpy()[:] = src
+    nx, ny, nz = hx.numpy(), hy.numpy(), hz.numpy()
+    e2e_times = []
+    if clocks_cb:
+        clocks_cb("start_e2e")
+    for i in range(args.warmup + args.steps):
+        for a, s in zip((nx, ny, nz), inputs):
+            np.copyto(a, s)
+        t = time.perf_counter()
+        ctx.build(nx, ny, nz, d, perm=None, heap_out=heap_np, ranges_out=ranges_np)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t)
+    if clocks_cb:
+        clocks_cb("end_e2e")
+    del hx, hy, hz, nx, ny, nz
+    h2d_gbs, d2h_gbs = measure_link(torch, dev, 4 * n)
+    heap_bytes = (2 * d - 1) * 52
+    h2d_bytes, d2h_bytes = 12 * n, 12 * n + heap_bytes + 8 * (2 * d - 1)
+    e2e_ms = 1e3 * sum(e2e_times) / len(e2e_times)
+    link_floor_ms = 1e3 * (h2d_bytes / (h2d_gbs * 1e9) + d2h_bytes / (d2h_gbs * 1e9))
+    e2e = {"value": n / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d_bytes,
+           "d2h_bytes_per_step": d2h_bytes,
+           "call": "orb_build(x,y,z host pinned, perm=NULL): reordered x,y,z + heap + ranges back",
+           "ms_per_step": e2e_ms,
+           "link_gbs": {"h2d": round(h2d_gbs, 1), "d2h": round(d2h_gbs, 1),
+                        "how": "one plain copy of 4n bytes each way between pinned host and HBM, "
+                               "CUDA events, same run"},
+           "link_floor_ms": round(link_floor_ms, 3),
+           "link_frac": round(link_floor_ms / e2e_ms, 4),
+           "link_note": "link_floor_ms = the step's bytes in and out at the measured link rates "
+                        "back to back; link_frac = that floor / the e2e step (1.0 = link-bound)"}
+
+    del x0, y0, z0, x, y, z, perm
+    torch.cuda.empty_cache()
+    return {
+        "n": n, "d": d, "kind": kind, "ms_total": ms_total, "ms_step": ms_total / args.steps,
+        "build_ms_device": statistics.median(i["device_ms"] for i in infos),
+        "with_perm_ms_per_step": round(perm_ms_step, 4), "tuning": tuning, "tuned_by": tuned_by,
+        "tune_s": round(tune_s, 2), "roofline": roofline, "count_left": count_left,
+        "kernels": kernels, "partition_ms_per_step": round(part_ms, 4), "launches": launches,
+        "e2e": e2e, "passes": infos[-1]["count_passes"], "warm_rebuild": warm_rb,
+        "parity_job": {"x": inputs[0], "y": inputs[1], "z": inputs[2],
+                       "instances": [{"offset": 0, "n": n, "d": d, "gpu": gpu_out}]},
+    }
 
 
 # ------------------------------------------------------------------------------------------
@@ -272,11 +566,19 @@ def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
     tuning, tuned_ms = ctx.autotune_batch(x0, y0, z0, inst, reps=3, device_pointers=True)
     tune_s = time.perf_counter() - t0
     t_batch, (parts, _, binfo) = timed(batch_step)
-    bperm = perm.cpu().numpy()
+    bperm = perm.cpu().numpy().view(np.uint32)
+    bx, by, bz = x.cpu().numpy(), y.cpu().numpy(), z.cpu().numpy()
     t_plain, _ = timed(plain_step)
-    pperm = perm.cpu().numpy()
+    pperm = perm.cpu().numpy().view(np.uint32)
     same = all(hb.tobytes() == hp.tobytes() and np.array_equal(rb, rp)
                for (hb, rb), (hp, rp) in zip(parts, outs)) and np.array_equal(bperm, pperm)
+    job_inst = []
+    for (hb, rb), ins in zip(parts, inst):
+        a, b = ins["offset"], ins["offset"] + ins["n"]
+        job_inst.append({**ins, "gpu": (hb.copy(), rb.copy(), bx[a:b], by[a:b], bz[a:b], bperm[a:b])})
+    job = {"x": x0.cpu().numpy(), "y": y0.cpu().numpy(), "z": z0.cpu().numpy(), "instances": job_inst}
+    del x0, y0, z0, x, y, z, perm
+    torch.cuda.empty_cache()
     return {
         "workload": "128 instances, particles log-uniform 2^14..2^22, leaves 2^6..2^12, "
                     "half uniform / half Plummer (seeded)",
@@ -289,7 +591,10 @@ def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
         "bit_exact_vs_plain": bool(same),
         "autotune": {"chosen": tuning, "default": default_tuning,
                      "median_build_ms": round(tuned_ms, 3), "tuning_s": round(tune_s, 2)},
-    }
+        "design": "each level's kernel sequence runs once over the cells of every instance "
+                  "(one launch per kernel kind and level for the whole batch), all levels "
+                  "captured in one CUDA graph",
+    }, job
 
 
 # ------------------------------------------------------------------------------------------
@@ -359,11 +664,23 @@ def bench_served(E, device, seed: int, rate: float = 2000.0, count: int = 2000):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def _section(r: dict, parity=None) -> dict:
+    """The per-workload keys of a run_plain result (clustered section)."""
+    return {"workload": workload_name(r["kind"], r["n"], r["d"]), "particles": r["n"],
+            "leaves": r["d"], "ms_per_step": round(r["ms_step"], 4),
+            "build_ms_device": round(r["build_ms_device"], 4),
+            "particles_per_s": r["n"] / (r["ms_step"] / 1e3),
+            "e2e": r["e2e"], "roofline": r["roofline"], "count_left": r["count_left"],
+            "partition_ms_per_step": r["partition_ms_per_step"],
+            "kernels_per_step_warmup": r["kernels"], "tuning": r["tuning"],
+            "with_perm_ms_per_step": r["with_perm_ms_per_step"], "parity": parity}
+
+
 def gpu_arm(args):
-    import numpy as np
     import torch
 
     import orb_gb300 as E
+    import replicas
 
     rank, world, local = dist_env()
     if world > 1:
@@ -374,137 +691,28 @@ def gpu_arm(args):
     n, d = args.particles, args.leaves
     ctx = E.Context(local, reserve_particles=n, reserve_leaves=d)
     dev = torch.device("cuda", local)
+    peak, peak_kind = measured_peak()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    # inputs generated on the device by the engine's seeded generator
-    x0, y0, z0 = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
-    ctx.generate(E.ORB_GEN_UNIFORM, SEED + rank, n, x0, y0, z0, device_pointers=True)
-    x, y, z = (torch.empty_like(x0) for _ in range(3))
-    perm = torch.empty(n, dtype=torch.int32, device=dev)
-    # cell heap and range map land in pinned host buffers (the API's host outputs)
-    heap_pin = torch.empty((2 * d - 1) * 52, dtype=torch.uint8, pin_memory=True)
-    ranges_pin = torch.empty((2 * d - 1) * 2, dtype=torch.int32, pin_memory=True)
-    heap_np = heap_pin.numpy().view(E.CELL_DTYPE)
-    ranges_np = ranges_pin.numpy().view(np.uint32).reshape(-1, 2)
-
-    def step(with_perm=False):
-        # the reference's outputs: reordered x,y,z, cell heap, range map (it has no
-        # permutation output; with_perm adds the engine's optional one)
-        x.copy_(x0)
-        y.copy_(y0)
-        z.copy_(z0)
-        torch.cuda.synchronize(dev)
-        return ctx.build(x, y, z, d, perm=perm if with_perm else None, device_pointers=True,
-                         heap_out=heap_np, ranges_out=ranges_np)
-
-    # launch parameters from the engine's autotuner on this workload (before any timing; the
-    # inputs are copied, every candidate's tree is checked equal)
-    t0 = time.perf_counter()
-    if args.tuning:
-        names = ("hist_blocks_per_sm", "part_blocks_per_sm", "tile_blocks_per_sm",
-                 "sparse_keys_per_tile", "cta_min_cells", "subtree_levels", "predict_sigmas")
-        ctx.set_tuning(**dict(zip(names, (int(v) for v in args.tuning.split(",")))))
-        tuning, tuned_by = ctx.get_tuning(), "--tuning"
-    else:
-        tuning, _ = ctx.autotune_batch(x0, y0, z0, [{"offset": 0, "n": n, "d": d}], reps=2,
-                                       device_pointers=True)
-        tuned_by = "orb_autotune_batch"
-    tune_s = time.perf_counter() - t0
-
-    # warm-up steps time every kernel: per-kernel breakdown and the dominant kernel
-    ctx.profile_reset(timing=True)
-    for _ in range(args.warmup):
-        step()
-    warm = ctx.profile()
-    warm_timed = {k: v for k, v in warm.items() if v["total_ms"] > 0}
-    dom = max(warm_timed, key=lambda k: warm_timed[k]["total_ms"])
     clocks = ClockSampler(gpu_id_for(local))
+    marks = {}
+
+    def mark(what):
+        if what == "start":
+            barrier()
+        marks[what] = time.perf_counter()
+
     time.sleep(0.5)
-    # timed steps: CUDA events only around the dominant kernel's launches (one untimed step
-    # first, so the build's CUDA graph is captured outside the timed region)
-    ctx.profile_reset(timing=[dom])
-    step()
-    ctx.profile_reset(timing=[dom])
-    barrier()
-    torch.cuda.synchronize(dev)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    tw0 = time.perf_counter()
-    ev0.record()
-    infos = []
-    for _ in range(args.steps):
-        infos.append(step().info)
-    ev1.record()
-    torch.cuda.synchronize(dev)
-    tw1 = time.perf_counter()
-    barrier()
-    ms_total = ev0.elapsed_time(ev1)
-    prof = ctx.profile()
-    import replicas
-    ms_total, _, value = replicas.whole_job(ms_total, n * args.steps)
+    head = run_plain(ctx, E, torch, dev, args, "uniform", n, d, SEED + rank, peak, peak_kind,
+                     args.tuning, clocks_cb=mark, with_warm=(rank == 0 and not args.no_warm))
+    ms_total, _, value = replicas.whole_job(head["ms_total"], n * args.steps)
     ms_step = ms_total / args.steps
-
-    # the same step with the optional permutation output (one more array moved per swap)
-    ctx.profile_reset(timing=False)
-    step(with_perm=True)
-    torch.cuda.synchronize(dev)
-    ev0.record()
-    for _ in range(args.steps):
-        step(with_perm=True)
-    ev1.record()
-    torch.cuda.synchronize(dev)
-    perm_ms_step = ev0.elapsed_time(ev1) / args.steps
-
-    # warm-started rebuild (labelled mode, not bit-identical with a cold build): the same
-    # particles displaced by sigma = 1e-3 (seeded, clamped to the box), rebuilt cold and from
-    # the previous tree's cuts
-    warm_rb = None
-    if rank == 0:
-        prev_heap = heap_np.copy()  # the tree of x0,y0,z0 (last step above)
-        g = torch.Generator(device=dev)
-        g.manual_seed(SEED + 11)
-        hi = float(np.nextafter(np.float32(0.5), np.float32(0)))
-        xd, yd, zd = ((a + 1e-3 * torch.randn(n, generator=g, device=dev)).clamp_(-0.5, hi)
-                      for a in (x0, y0, z0))
-        cold_ms, warm_ms, winfo = [], [], None
-        for i in range(args.warmup + args.steps):
-            for dst, src in ((x, xd), (y, yd), (z, zd)):
-                dst.copy_(src)
-            c = ctx.build(x, y, z, d, perm=None, device_pointers=True)
-            for dst, src in ((x, xd), (y, yd), (z, zd)):
-                dst.copy_(src)
-            w = ctx.build_warm(x, y, z, d, prev_heap, WARM_WIDTH, perm=None, device_pointers=True)
-            if i >= args.warmup:
-                cold_ms.append(c.info["device_ms"])
-                warm_ms.append(w.info["device_ms"])
-                winfo = w.info
-        warm_rb = {"workload": f"{WORKLOAD}, particles displaced by N(0, 1e-3^2) per coordinate",
-                "width": WARM_WIDTH, "cold_build_ms": round(statistics.median(cold_ms), 3),
-                "warm_build_ms": round(statistics.median(warm_ms), 3),
-                "speedup": round(statistics.median(cold_ms) / statistics.median(warm_ms), 3),
-                "warm_cells": winfo["warm_cells"], "warm_resets": winfo["warm_resets"],
-                "note": "labelled mode: a valid ORB tree, not bit-identical with the cold build"}
-
-    # end to end through the C ABI with pinned host buffers
-    hx, hy, hz = (torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3))
-    hx.copy_(x0.cpu()); hy.copy_(y0.cpu()); hz.copy_(z0.cpu())
-    src = [t.numpy().copy() for t in (hx, hy, hz)]
-    nx, ny, nz = hx.numpy(), hy.numpy(), hz.numpy()
-    e2e_times = []
-    te0 = time.perf_counter()
-    for i in range(args.warmup + args.steps):
-        for a, s in zip((nx, ny, nz), src):
-            np.copyto(a, s)
-        t = time.perf_counter()
-        ctx.build(nx, ny, nz, d, perm=None, heap_out=heap_np, ranges_out=ranges_np)
-        if i >= args.warmup:
-            e2e_times.append(time.perf_counter() - t)
-    te1 = time.perf_counter()
-    e2e_ms, _, e2e_value = replicas.whole_job(1e3 * sum(e2e_times), n * len(e2e_times))
-    e2e_s = e2e_ms / 1e3
+    e2e_ms, _, e2e_value = replicas.whole_job(head["e2e"]["ms_per_step"], n)
+    head["e2e"]["value"] = e2e_value
+    clock_summary = clocks.summary(marks["start"], marks["end_e2e"])
     clocks.stop()
 
     if rank != 0:
@@ -512,91 +720,65 @@ def gpu_arm(args):
             torch.distributed.destroy_process_group()
         return 0
 
-    # roofline of the dominant kernel (its events in the timed region)
-    peak, peak_kind = measured_peak()
-    dk = prof[dom]
-    achieved = dk["bytes"] / (dk["total_ms"] / 1e3) / 1e9
-    kern_ms_total = sum(v["total_ms"] for v in warm_timed.values())
-    dom_share = warm_timed[dom]["total_ms"] / kern_ms_total
-    ratio = traffic_ratio(dom)
-    roofline = {
-        "bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-        "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-        "traffic": (ratio * dk["bytes"] / dk["launches"]) if ratio else None,
-        "traffic_source": "ncu dram bytes per algorithmic byte, 2^24/2^13 capture scaled per unit"
-                          if ratio else None,
-        "dram_gbs_equivalent": round(achieved * ratio, 1) if ratio else None,
-        "bytes_per_launch": dk["bytes"] / dk["launches"],
-        "ms_per_launch": dk["total_ms"] / dk["launches"],
-        "share_of_kernel_time": round(dom_share, 4),
-    }
-    wsteps = max(args.warmup, 1)
-    # count-left (the kernel family held to 0.60 of the HBM peak): every launch that counts
-    # keys below a cut in the warm-up steps, against the measured HBM peak; the last levels
-    # run inside k_subtree (bisection and partition of one cell per CTA), listed in
-    # kernels_per_step_warmup
-    cl_names = [k for k in ("count_left_hist", "bisect_tile", "count_left_sample",
-                            "count_left_sample_pick") if k in warm]
-    cl_bytes = sum(warm[k]["bytes"] for k in cl_names) / wsteps
-    cl_ms = sum(warm[k]["total_ms"] for k in cl_names) / wsteps
-    cl_gbs = cl_bytes / (cl_ms / 1e3) / 1e9 if cl_ms else None
-    count_left = {"kernels": cl_names, "bytes_per_step": cl_bytes, "ms_per_step": round(cl_ms, 4),
-                  "achieved": round(cl_gbs, 1) if cl_gbs else None, "peak": peak, "unit": "GB/s",
-                  "frac": round(cl_gbs / peak, 4) if cl_gbs else None,
-                  "peak_source": f"{peak_kind} hbm_gbs",
-                  "bytes": "4 B per key read + 4 B per key compacted (algorithmic, engine counters)"}
-    kernels = {k: {"launches": v["launches"] // wsteps,
-                   "ms": round(v["total_ms"] / wsteps, 4),
-                   "GBps": round(v["bytes"] / (v["total_ms"] / 1e3) / 1e9, 1) if v["total_ms"] else None}
-               for k, v in warm.items()}
-    launches = sum(v["launches"] for v in prof.values())
-
+    clustered = None
+    jobs = {"headline": head.pop("parity_job")}
+    if not args.no_clustered:
+        cn, cd = CLUSTERED
+        cl = run_plain(ctx, E, torch, dev, args, "plummer", cn, cd, SEED + 33, peak, peak_kind, None)
+        jobs["clustered"] = cl.pop("parity_job")
+        clustered = cl
     batched = None
     if not args.no_batched:
-        batched = bench_batched(ctx, E, torch, dev, max(2, min(args.steps, 5)), 1, SEED + 77)
+        batched, jobs["batched"] = bench_batched(ctx, E, torch, dev, max(2, min(args.steps, 5)), 1,
+                                                 SEED + 77)
+    ctx.close()
     served = None
     if not args.no_served:
-        del x0, y0, z0, x, y, z  # give the server's arena the memory
         torch.cuda.empty_cache()
         served = bench_served(E, local, SEED + 99)
 
+    # CPU leg: the checker on the benchmark's own inputs, then the timed CPU baseline
+    parity = {}
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = run_cpu(1, 0, budget_s=40.0)
+        for name, job in jobs.items():
+            parity[name] = check_parity(job)
+        jobs.clear()
+        cpu = run_cpu(N_PARTICLES, LEAVES, 1, 0, budget_s=40.0)
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if clustered is not None:
+        clustered = _section(clustered, parity.get("clustered"))
+    if batched is not None:
+        batched["parity"] = parity.get("batched")
 
-    heap_bytes = (2 * d - 1) * 52
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform, engine generator)",
-        "config": {"workload": WORKLOAD, "particles": n, "leaves": d, "levels": 16,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "inputs 1.5 GB > 129 MB L2 (no flush needed)",
-                   "step": "d2d restore of x,y,z + orb_build (device pointers)",
-                   "outputs": "reordered x,y,z + cell heap + range map (as the reference; "
-                              "optional permutation off, timed separately as with_perm)"},
-        "build_ms_device": statistics.median(i["device_ms"] for i in infos),
-        "tuning": {"chosen": tuning, "by": tuned_by, "tuning_s": round(tune_s, 2)},
-        "with_perm_ms_per_step": round(perm_ms_step, 4),
-        "warm_rebuild": warm_rb,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
-                "d2h_bytes_per_step": 12 * n + heap_bytes + 8 * (2 * d - 1),
-                "call": "orb_build(x,y,z host pinned, perm=NULL): reordered x,y,z + heap + ranges back",
-                "ms_per_step": 1e3 * e2e_s / len(e2e_times)},
-        "roofline": roofline,
-        "count_left": count_left,
-        "kernels_per_step_warmup": kernels,
-        "gpu_launches": launches,
+        "config": workload_config(n, d, world),
+        "step": {"what": "d2d restore of x,y,z + orb_build (device pointers)",
+                 "outputs": "reordered x,y,z + cell heap + range map (as the reference; the "
+                            "optional permutation is off, timed separately as with_perm)"},
+        "parity": parity.get("headline"),
+        "build_ms_device": head["build_ms_device"],
+        "tuning": {"chosen": head["tuning"], "by": head["tuned_by"], "tuning_s": head["tune_s"]},
+        "with_perm_ms_per_step": head["with_perm_ms_per_step"],
+        "warm_rebuild": head["warm_rebuild"],
+        "e2e": head["e2e"],
+        "roofline": head["roofline"],
+        "count_left": head["count_left"],
+        "partition_ms_per_step": head["partition_ms_per_step"],
+        "kernels_per_step_warmup": head["kernels"],
+        "gpu_launches": head["launches"],
         "cpu_baseline": cpu,
+        "clustered": clustered,
         "batched": batched,
         "served": served,
-        "clocks": clocks.summary(tw0, te1),
-        "bisection_passes_per_build": infos[-1]["count_passes"],
+        "clocks": clock_summary,
+        "bisection_passes_per_build": head["passes"],
     }
     print(json.dumps(line), flush=True)
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -610,9 +792,12 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--particles", type=int, default=N_PARTICLES)
     ap.add_argument("--leaves", type=int, default=LEAVES)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU leg (timed baseline and the oracle's parity check)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-clustered", action="store_true")
+    ap.add_argument("--no-warm", action="store_true")
     ap.add_argument("--tuning", default=None,
                     help="hist,part,tile,sparse,cta,subtree[,predict]: use this launch tuning for the headline "
                          "instead of autotuning it (profiling runs reuse a chosen setting)")
