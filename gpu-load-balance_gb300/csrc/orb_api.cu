@@ -696,10 +696,34 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     return ORB_OK;
 }
 
+// After a failed build from host memory: the copies the build queued may still be reading
+// or writing the caller's arrays, so wait for them before the caller gets control back.
+static void drain_host_copies(orb_ctx *ctx) {
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->yz_pending = false;
+    cudaGetLastError();
+}
+
+static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                               uint32_t levels, const float lower[3], const float upper[3],
+                               orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                               orb_build_info *info);
+
 orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
                      uint32_t levels, const float lower[3], const float upper[3],
                      orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
                      orb_build_info *info) {
+    const orb_status st = build_single(ctx, x, y, z, n, d, levels, lower, upper, heap, ranges,
+                                       perm, flags, info);
+    if (st != ORB_OK && ctx && !(flags & ORB_DEVICE_POINTERS)) drain_host_copies(ctx);
+    return st;
+}
+
+static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
+                               uint32_t levels, const float lower[3], const float upper[3],
+                               orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+                               orb_build_info *info) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
     if (flags & ~ORB_DEVICE_POINTERS) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown flags");
@@ -1345,8 +1369,10 @@ orb_status orb_build_batch(orb_ctx *ctx, float *x, float *y, float *z, uint64_t 
                            const orb_batch_instance *inst, uint32_t k, orb_cell_t *heaps,
                            uint32_t *ranges, uint32_t *perm, uint32_t flags,
                            orb_build_info *info) {
-    return build_batch_impl(ctx, x, y, z, n_total, inst, k, nullptr, nullptr, heaps, ranges, perm,
-                            flags, info);
+    const orb_status st = build_batch_impl(ctx, x, y, z, n_total, inst, k, nullptr, nullptr, heaps,
+                                           ranges, perm, flags, info);
+    if (st != ORB_OK && ctx && !(flags & ORB_DEVICE_POINTERS)) drain_host_copies(ctx);
+    return st;
 }
 
 orb_status orb_build_batch_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n_total,
@@ -1360,8 +1386,10 @@ orb_status orb_build_batch_warm(orb_ctx *ctx, float *x, float *y, float *z, uint
     for (uint32_t i = 0; i < k; ++i)
         if (!(widths[i] >= 0.f) || !std::isfinite(widths[i]))
             return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "widths must be finite and >= 0");
-    return build_batch_impl(ctx, x, y, z, n_total, inst, k, prev_heaps, widths, heaps, ranges, perm,
-                            flags, info);
+    const orb_status st = build_batch_impl(ctx, x, y, z, n_total, inst, k, prev_heaps, widths,
+                                           heaps, ranges, perm, flags, info);
+    if (st != ORB_OK && !(flags & ORB_DEVICE_POINTERS)) drain_host_copies(ctx);
+    return st;
 }
 
 orb_status orb_build_warm(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,

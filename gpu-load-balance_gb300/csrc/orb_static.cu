@@ -34,7 +34,9 @@ DeviceSetup g_setup[kMaxDevices];
 
 // Once per device, with that device current: resolve the array's device address. Host
 // code must not pass `g_count_scratch` itself to a kernel: on the host that name is a
-// host-side stand-in, not a device address.
+// host-side stand-in, not a device address. The address is kept for the life of the
+// process, so the entry point must not be called on a device after cudaDeviceReset there
+// (the module, and with it the array, is loaded again at another address).
 cudaError_t setup_device(int dev, DeviceSetup *out) {
     std::lock_guard<std::mutex> g(g_setup_mu);
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;

@@ -363,6 +363,8 @@ int orb_profile_read(orb_ctx *ctx, orb_kernel_stat *out, int max_entries);
  * held until the process exits); n_cells above that returns ORB_ERR_CAPACITY. The call
  * uses the calling thread's current device. Its first call on a device resolves the
  * array's address (cudaGetSymbolAddress); make that first call before any stream capture.
+ * That address is kept until the process exits: do not call it on a device after a
+ * cudaDeviceReset of that device.
  * Every call shares the one array (the kernels clear it first), so calls that overlap on
  * the GPU, on different streams or threads, race and must be serialised by the caller.
  */
