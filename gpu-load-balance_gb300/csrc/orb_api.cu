@@ -52,11 +52,6 @@ struct DevBuf {
     }
 };
 
-int log2_exact(uint32_t d) {
-    int k = 0;
-    while ((1u << k) < d) ++k;
-    return k;
-}
 
 
 }  // namespace
@@ -102,6 +97,8 @@ struct orb_ctx {
     DevBuf<int> hint_axis;
     DevBuf<uint8_t> warm;
     DevBuf<uint32_t> sub_flag;  // subtree path taken (one word)
+    DevBuf<uint32_t> w;         // weighted builds from host memory: the weights
+    DevBuf<unsigned long long> whist, wbelow, wtot;  // weighted builds: per-cell weight sums
     BuildCounters *h_counters = nullptr;  // pinned
     uint32_t *h_sub_flag = nullptr;       // pinned: the subtree path was taken
 
@@ -422,7 +419,8 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
                           (const void *)v.pt_ge_pre, (const void *)v.pt_le_pre, (const void *)v.pt_status,
                           (const void *)v.part_s, (const void *)v.part_i, (const void *)v.part_le,
-                          (const void *)v.pred, (const void *)v.counters})
+                          (const void *)v.pred, (const void *)v.counters, (const void *)v.wt,
+                          (const void *)v.whist, (const void *)v.wbelow, (const void *)v.wtot})
         key_add(key, p);
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
@@ -524,7 +522,16 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
         run_kernel(ctx, kKPlan, v, 1);
         run_kernel(ctx, kKTileMap, v, pass_grid(ctx));
         if (v.hint) run_kernel(ctx, kKWarmStart, v, 1);  // warm build: hinted brackets
-        if (ctx->tune.cta_min_cells && !v.hint && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
+        if (v.wt) {
+            // weighted build: every cell through the weighted passes (kWPasses reach the cap)
+            run_kernel(ctx, kKWStart, v, pass_grid(ctx));
+            for (int pass = 0; pass < kWPasses; ++pass) {
+                v.pass = pass;
+                run_kernel(ctx, kKWHist, v, pass_grid(ctx));
+                run_kernel(ctx, kKWResolve, v, 0);
+                ++*passes;
+            }
+        } else if (ctx->tune.cta_min_cells && !v.hint && (uint32_t)v.C >= ctx->tune.cta_min_cells) {
             // many cells: one CTA bisects one cell, no host round trip
             run_kernel(ctx, kKBisectCta, v, std::min(v.C, ctx->num_sms * 4));
         } else {
@@ -680,6 +687,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
         ctx->tune_work[a].release();
     }
     ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release(); ctx->sub_flag.release();
+    ctx->w.release(); ctx->whist.release(); ctx->wbelow.release(); ctx->wtot.release();
     ctx->listed.release(); ctx->cmp_bad.release(); ctx->cmp_off.release(); ctx->cmp_cnt.release();
     ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -705,24 +713,38 @@ static void drain_host_copies(orb_ctx *ctx) {
     cudaGetLastError();
 }
 
-static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
-                               uint32_t levels, const float lower[3], const float upper[3],
-                               orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *w,
+                               bool weighted, uint64_t n, uint32_t d, uint32_t levels,
+                               const float lower[3], const float upper[3], orb_cell_t *heap,
+                               uint32_t *ranges, uint32_t *perm, uint32_t flags,
                                orb_build_info *info);
 
 orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
                      uint32_t levels, const float lower[3], const float upper[3],
                      orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
                      orb_build_info *info) {
-    const orb_status st = build_single(ctx, x, y, z, n, d, levels, lower, upper, heap, ranges,
-                                       perm, flags, info);
+    const orb_status st = build_single(ctx, x, y, z, nullptr, false, n, d, levels, lower, upper,
+                                       heap, ranges, perm, flags, info);
     if (st != ORB_OK && ctx && !(flags & ORB_DEVICE_POINTERS)) drain_host_copies(ctx);
     return st;
 }
 
-static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
-                               uint32_t levels, const float lower[3], const float upper[3],
-                               orb_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint32_t flags,
+orb_status orb_build_weighted(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *w, uint64_t n,
+                              uint32_t d, uint32_t levels, const float lower[3],
+                              const float upper[3], orb_cell_t *heap, uint32_t *ranges,
+                              uint32_t *perm, uint32_t flags, orb_build_info *info) {
+    if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
+    if (n > 0 && !w) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null weights");
+    const orb_status st = build_single(ctx, x, y, z, w, true, n, d, levels, lower, upper, heap,
+                                       ranges, perm, flags, info);
+    if (st != ORB_OK && !(flags & ORB_DEVICE_POINTERS)) drain_host_copies(ctx);
+    return st;
+}
+
+static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *w,
+                               bool weighted, uint64_t n, uint32_t d, uint32_t levels,
+                               const float lower[3], const float upper[3], orb_cell_t *heap,
+                               uint32_t *ranges, uint32_t *perm, uint32_t flags,
                                orb_build_info *info) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
@@ -740,7 +762,7 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
                     "ceil(log2 d) - 1 (other d)");
     const bool dev = (flags & ORB_DEVICE_POINTERS) != 0;
     if (dev && n > 0 && (!is_device_ptr(x) || !is_device_ptr(y) || !is_device_ptr(z) ||
-                         (perm && !is_device_ptr(perm))))
+                         (perm && !is_device_ptr(perm)) || (w && !is_device_ptr(w))))
         return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "ORB_DEVICE_POINTERS set but a pointer is not device memory");
 
     ORB_CUDA(cudaSetDevice(ctx->device));
@@ -750,7 +772,14 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
     orb_status st = ensure_level_buffers(ctx, n, max_cells, heap_cells);
     if (st != ORB_OK) return st;
     ORB_CUDA(ctx->idx.ensure(n + 1));
+    if (weighted) {
+        ORB_CUDA(ctx->whist.ensure((size_t)max_cells * kWBins));
+        ORB_CUDA(ctx->wbelow.ensure(max_cells));
+        ORB_CUDA(ctx->wtot.ensure(max_cells));
+        if (!dev) ORB_CUDA(ctx->w.ensure(n + 1));
+    }
     float *dx = x, *dy = y, *dz = z;
+    uint32_t *dw = weighted ? (dev ? w : ctx->w.p) : nullptr;
     cudaStream_t s = ctx->stream;
     float h2d_ms = 0.f, d2h_ms = 0.f;
     ctx->yz_pending = false;
@@ -768,6 +797,8 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
             if (!ctx->copy_stream) ORB_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
             if (!ctx->yz_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->yz_ready, cudaEventDisableTiming));
             ORB_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(float), cudaMemcpyHostToDevice, s));
+            if (weighted)  // the root level's bisection reads x and the weights
+                ORB_CUDA(cudaMemcpyAsync(dw, w, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
             ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[2], 0));
             ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
             ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
@@ -781,6 +812,12 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
     ORB_CUDA(cudaEventRecord(ctx->ev[0], s));
     Level v = make_level(ctx, dx, dy, dz);
     if (!perm) v.idx = nullptr;  // no permutation asked for: only x, y, z move
+    if (weighted) {
+        v.wt = dw;
+        v.whist = ctx->whist.p;
+        v.wbelow = ctx->wbelow.p;
+        v.wtot = ctx->wtot.p;
+    }
     std::vector<LevelDesc> lv;
     for (uint32_t l = 1; l <= levels; ++l)
         lv.push_back({sl.first(l), nullptr, sl.count(l)});  // src/orbit.cpp:104-107
@@ -793,8 +830,8 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
         key_add_f(key, lower[a]);
         key_add_f(key, upper[a]);
     }
-    // subtrees finish complete trees only: d a power of two, built to its leaves
-    const int sub_from = subtree_from(ctx, lv, n, sl.pow2 && levels == sl.depth);
+    // subtrees finish complete unweighted trees only: d a power of two, built to its leaves
+    const int sub_from = subtree_from(ctx, lv, n, !weighted && sl.pow2 && levels == sl.depth);
     if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
     key.push_back((uint64_t)(int64_t)sub_from);
     // pinned host outputs of a build that plans subtrees: the subtree kernel writes every
@@ -834,6 +871,8 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint6
             ORB_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, s));
             ORB_CUDA(cudaMemcpyAsync(z, dz, n * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
+        if (n && weighted)  // the weights, reordered with their particles
+            ORB_CUDA(cudaMemcpyAsync(w, dw, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     }
     if (perm && n && !written)
         ORB_CUDA(cudaMemcpyAsync(perm, ctx->idx.p, n * sizeof(uint32_t),

@@ -39,6 +39,13 @@ constexpr int kSubtreeBlocksPerSm = 4;  // CTAs of the subtree kernel per SM (it
 constexpr uint32_t kSubMaxParticles = ORB_SUB_MAX;  // largest cell one subtree CTA takes
 constexpr int kSubMaxLevels = 6;              // deepest tree one subtree CTA finishes
 
+// Weighted builds: every active cell's bracket is binned into a midpoint tree of this depth
+// per pass (its weights summed per bin), so kWPasses passes reach the 32-iteration cap.
+constexpr int kWBinsLog2 = 8;
+constexpr int kWBins = 1 << kWBinsLog2;
+constexpr int kWPasses = 4;
+static_assert(kWPasses * kWBinsLog2 >= 32, "the weighted passes reach the iteration cap");
+
 // kSmall: at most kWarpKeys keys (one warp bisects it); kOneTile: at most kTile keys (one CTA)
 enum CellState : uint8_t { kActive = 0, kFound = 1, kCapped = 2, kSmall = 3, kOneTile = 4 };
 constexpr int kWarpKeys = 1024;      // cells up to this size bisect in one warp's registers
@@ -67,6 +74,9 @@ enum Kernel : int {
     kKSubtree,
     kKSample,
     kKSamplePick,
+    kKWStart,
+    kKWHist,
+    kKWResolve,
     kNumKernels
 };
 static_assert(kNumKernels <= 32, "BuildCounters::bytes holds 32 kernel kinds");
@@ -152,6 +162,13 @@ struct Level {
     // cell's final particles there, overlapping the device-to-host transfer with the last levels
     float *hx, *hy, *hz;
     uint32_t *hperm;
+    // weighted builds (null otherwise): an integer weight per particle, moved with it, and
+    // per cell of the level its weight bins (kWBins), the weight below its bracket and its
+    // total weight
+    uint32_t *wt;
+    unsigned long long *whist;
+    unsigned long long *wbelow;
+    unsigned long long *wtot;
     BuildCounters *counters;
 };
 
@@ -176,6 +193,24 @@ __device__ __forceinline__ int convergence(uint32_t count_left, uint32_t count, 
     int difference = __float2int_rz(diff);
     if (difference > -3 && difference < 3) return 0;
     return difference > 0 ? 1 : -1;
+}
+
+// The weighted test (no counterpart in the reference, whose thesis specifies weighted ORB,
+// documentation/notes.tex:259-271, and whose code never implements it): the reference's
+// |W_left - ratio W| < 3 (src/orbit.cpp:204-208) with the tolerance scaled by the cell's
+// mean weight W/n, exact in 128-bit integers: D = k W_left - ceil(k/2) W for k leaves;
+// found when D == 0 or n |D| < 3 k W; else +1 (D > 0, the right margin moves) or -1. With
+// unit weights: |cl - ratio c| < 3 exactly, the reference's float32 test wherever that test
+// is exact (fewer than 2^24 particles, an even k).
+__device__ __forceinline__ int convergence_weighted(unsigned long long w_left,
+                                                    unsigned long long w_cell, uint32_t n,
+                                                    int32_t n_leaf) {
+    const __int128 k = n_leaf, half = (n_leaf + 1) / 2;
+    const __int128 D = k * (__int128)w_left - half * (__int128)w_cell;
+    const unsigned __int128 ad = (unsigned __int128)(D < 0 ? -D : D);
+    if (D == 0 || (unsigned __int128)n * ad < (unsigned __int128)3 * (unsigned __int128)k * w_cell)
+        return 0;
+    return D > 0 ? 1 : -1;
 }
 
 __device__ __forceinline__ const float *axis_keys(const Level &v, int axis) {

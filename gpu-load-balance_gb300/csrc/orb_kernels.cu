@@ -29,7 +29,8 @@ const char *const kKernelNames[kNumKernels] = {
     "init", "plan", "count_left_hist", "bisect_resolve", "part_classify", "part_scan",
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
     "tile_map", "bisect_tile", "warm_start", "subtree_check", "subtree",
-    "count_left_sample", "count_left_sample_pick"};
+    "count_left_sample", "count_left_sample_pick", "weighted_start", "count_left_weighted",
+    "bisect_resolve_weighted"};
 
 namespace {
 
@@ -2152,6 +2153,11 @@ __device__ __forceinline__ void swap_particles(const Level &v, uint32_t a, uint3
         v.idx[a] = ib;
         v.idx[b] = ia;
     }
+    if (v.wt) {
+        const uint32_t wa = v.wt[a], wb = v.wt[b];
+        v.wt[a] = wb;
+        v.wt[b] = wa;
+    }
 }
 
 // Largest u in [lo, hi] with pre[u] - base <= r, for a nondecreasing pre with
@@ -2183,6 +2189,7 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #ifndef ORB_SWAP_MIN_BLOCKS
 #define ORB_SWAP_MIN_BLOCKS 4
 #endif
+template <bool kWt>  // kWt: weighted builds, whose weights move with their particles
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
@@ -2218,7 +2225,7 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
         for (uint32_t j0 = 0; j0 < cnt; j0 += kB * blockDim.x) {
             uint32_t pa[kB], pb[kB];
             float xa[kB], xb[kB], ya[kB], yb[kB], za[kB], zb[kB];
-            uint32_t ia[kB], ib[kB];
+            uint32_t ia[kB], ib[kB], wa[kB], wb[kB];
 #pragma unroll
             for (int q = 0; q < kB; ++q) {
                 const uint32_t j = j0 + q * blockDim.x + threadIdx.x;
@@ -2236,6 +2243,10 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                         ia[q] = v.idx[pa[q]];
                         ib[q] = v.idx[pb[q]];
                     }
+                    if constexpr (kWt) {
+                        wa[q] = v.wt[pa[q]];
+                        wb[q] = v.wt[pb[q]];
+                    }
                 }
             }
 #pragma unroll
@@ -2251,13 +2262,18 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                     v.idx[pa[q]] = ib[q];
                     v.idx[pb[q]] = ia[q];
                 }
+                if constexpr (kWt) {
+                    v.wt[pa[q]] = wb[q];
+                    v.wt[pb[q]] = wa[q];
+                }
             }
         }
         bytes += cnt;
         __syncthreads();
     }
-    // per pair: both elements of x, y, z (and idx) read and written
-    if (threadIdx.x == 0 && bytes) add_bytes(v, kKPartSwap, (v.idx ? 64ull : 48ull) * bytes);
+    // per pair: both elements of x, y, z (and idx, weights) read and written
+    if (threadIdx.x == 0 && bytes)
+        add_bytes(v, kKPartSwap, (48ull + (v.idx ? 16ull : 0ull) + (kWt ? 16ull : 0ull)) * bytes);
 }
 
 __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {
@@ -2783,6 +2799,156 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
 }
 
 // ------------------------------------------------------------------------------------
+// Weighted builds: the reference's bisection loop on integer weight sums instead of counts
+// (the thesis's weighted ORB, documentation/notes.tex:259-271; never implemented by the
+// reference). Per level: every cell starts active; kWPasses passes each bin the weights of
+// every active cell's bracket into its midpoint tree of depth kWBinsLog2 (the exact
+// descent: the reference's own cuts) and sum the weights below the bracket; a resolve per
+// cell replays up to kWBinsLog2 iterations of the loop on the prefix sums with the weighted
+// test. Integer sums: the same results in any order.
+// ------------------------------------------------------------------------------------
+__global__ void k_wstart(Level v) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < (uint32_t)v.C;
+         c += gridDim.x * blockDim.x) {
+        v.state[c] = kActive;
+        v.iters[c] = 0;
+        v.wbelow[c] = 0ull;
+        v.wtot[c] = 0ull;
+    }
+    const uint64_t nb = (uint64_t)v.C * kWBins;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nb;
+         j += (uint64_t)gridDim.x * blockDim.x)
+        v.whist[j] = 0ull;
+}
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x,
+                                                            unsigned long long *sh) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = x;
+    __syncthreads();
+    unsigned long long t = 0;
+    for (int w = 0; w < nw; ++w) t += sh[w];
+    return t;
+}
+
+__global__ void __launch_bounds__(kThreads) k_whist(Level v) {
+    __shared__ unsigned long long s_bins[kWBins];
+    __shared__ unsigned long long s_red[kThreads / 32];
+    const uint32_t total = v.tile_off[v.C];
+    unsigned long long bytes = 0;
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const TileRef tr = tile_ref(v, t);
+        if (v.state[tr.c] != kActive) continue;  // block-uniform
+        const orb_cell_t &cell = v.heap[tr.slot];
+        const float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+        const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+        for (uint32_t j = threadIdx.x; j < (uint32_t)kWBins; j += blockDim.x) s_bins[j] = 0ull;
+        __syncthreads();
+        unsigned long long below = 0, tot = 0;
+        for (uint32_t p = tr.e0 + threadIdx.x; p < tr.e1; p += blockDim.x) {
+            const float k = __ldg(keys + p);
+            const uint32_t w = __ldg(v.wt + p);
+            tot += w;
+            if (k < L)
+                below += w;
+            else if (k < R && w)
+                atomicAdd(&s_bins[tree_bin(k, L, R, kWBinsLog2)], (unsigned long long)w);
+        }
+        below = block_sum_u64(below, s_red);
+        tot = block_sum_u64(tot, s_red);
+        __syncthreads();
+        unsigned long long *g = v.whist + (size_t)tr.c * kWBins;
+        for (uint32_t j = threadIdx.x; j < (uint32_t)kWBins; j += blockDim.x)
+            if (s_bins[j]) atomicAdd(&g[j], s_bins[j]);
+        if (threadIdx.x == 0) {
+            if (below) atomicAdd(&v.wbelow[tr.c], below);
+            if (v.pass == 0 && tot) atomicAdd(&v.wtot[tr.c], tot);
+            bytes += 8ull * (tr.e1 - tr.e0);
+        }
+        __syncthreads();  // s_bins reused by the next tile
+    }
+    if (threadIdx.x == 0 && bytes) add_bytes(v, kKWHist, bytes);
+}
+
+// A warp per cell: the replay of up to kWBinsLog2 iterations of src/orbit.cpp:146-232 on the
+// pass's weight bins, with the weighted test; the bins and the weight below are cleared for
+// the next pass.
+__global__ void __launch_bounds__(kThreads) k_wresolve(Level v) {
+    __shared__ unsigned long long s_pre[kThreads / 32][kWBins];
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= v.C) return;
+    if (v.state[c] != kActive) return;  // warp-uniform
+    unsigned long long *pre = s_pre[threadIdx.x >> 5];
+    unsigned long long *g = v.whist + (size_t)c * kWBins;
+    constexpr int kPer = kWBins / 32;
+    unsigned long long loc[kPer], run = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        loc[j] = g[lane * kPer + j];
+        g[lane * kPer + j] = 0ull;
+        run += loc[j];
+    }
+    // exclusive prefix of the lanes' runs
+    unsigned long long inc = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    unsigned long long acc = inc - run;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        pre[lane * kPer + j] = acc;
+        acc += loc[j];
+    }
+    __syncwarp();
+    const int slot = level_slot(v, c);
+    orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const unsigned long long W = v.wtot[c], below = v.wbelow[c];
+    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    uint32_t it = v.iters[c], pos = 0, width = kWBins;
+    uint8_t st = kActive;
+    for (int step = 0; step < kWBinsLog2; ++step) {
+        if (it >= (uint32_t)kMaxIterations) {
+            st = kCapped;
+            break;
+        }
+        const uint32_t half = width >> 1;
+        const unsigned long long wl = below + pre[pos + half];
+        ++it;
+        const int dir = convergence_weighted(wl, W, n, cell.nLeafCells);
+        if (dir == 0) {
+            st = kFound;
+            break;
+        }
+        const float cut = mid_cut(L, R);
+        if (dir > 0) {
+            R = cut;
+        } else {
+            L = cut;
+            pos += half;
+        }
+        width = half;
+    }
+    if (st == kActive && it >= (uint32_t)kMaxIterations) st = kCapped;
+    __syncwarp();
+    if (lane == 0) {
+        cell.cutMarginLeft = L;
+        cell.cutMarginRight = R;
+        cell.foundCut = st == kFound ? 1 : 0;
+        v.iters[c] = (uint8_t)it;
+        v.state[c] = st;
+        v.wbelow[c] = 0ull;
+        if (st != kActive) atomicMax(&v.counters->max_iters, it);
+        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+    }
+}
+
+// ------------------------------------------------------------------------------------
 // Service count-left: one plain pass at getCut() per cell, found cells skipped.
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_count_left(Level v) {
@@ -2978,7 +3144,17 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKPartCells:
             k_part_cells<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
             break;
-        case kKPartSwap: k_part_swap<<<grid, kThreads, 0, st>>>(v); break;
+        case kKPartSwap:
+            if (v.wt)
+                k_part_swap<true><<<grid, kThreads, 0, st>>>(v);
+            else
+                k_part_swap<false><<<grid, kThreads, 0, st>>>(v);
+            break;
+        case kKWStart: k_wstart<<<grid, kThreads, 0, st>>>(v); break;
+        case kKWHist: k_whist<<<grid, kThreads, 0, st>>>(v); break;
+        case kKWResolve:
+            k_wresolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
+            break;
         case kKPartFinish:
             k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, arg);
             break;

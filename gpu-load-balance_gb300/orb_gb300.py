@@ -68,7 +68,7 @@ EXPORTS = [
     "orb_server_submit_generate", "orb_server_submit_rebalance", "orb_server_wait", "orb_server_poll",
     "orb_server_fetch", "orb_server_release", "orb_server_get_stats", "orb_get_tuning",
     "orb_set_tuning", "orb_autotune_batch", "orb_build_batch_warm", "orb_build_warm",
-    "orb_server_submit_rebalance_warm", "orb_test_set_scan_wait",
+    "orb_server_submit_rebalance_warm", "orb_test_set_scan_wait", "orb_build_weighted",
 ]
 
 ORB_STATIC_MAX_CELLS = 65536
@@ -226,6 +226,9 @@ def load(path: str | None = None):
     L.orb_build.restype = ctypes.c_int
     L.orb_build.argtypes = [vp, vp, vp, vp, u64, u32, u32, vp, vp, vp, vp, vp, u32,
                             ctypes.POINTER(BuildInfo)]
+    L.orb_build_weighted.restype = ctypes.c_int
+    L.orb_build_weighted.argtypes = [vp, vp, vp, vp, vp, u64, u32, u32, vp, vp, vp, vp, vp, u32,
+                                     ctypes.POINTER(BuildInfo)]
     L.orb_load_particles.restype = ctypes.c_int
     L.orb_load_particles.argtypes = [vp, vp, vp, vp, u64, u32, u32]
     L.orb_store_particles.restype = ctypes.c_int
@@ -372,6 +375,25 @@ class Context:
         st = self.lib.orb_build(self.h, _ptr(x), _ptr(y), _ptr(z), n, d, levels, lo.ctypes.data,
                                 hi.ctypes.data, heap.ctypes.data, ranges.ctypes.data, _ptr(perm),
                                 ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
+        self._check(st)
+        return BuildResult(heap, ranges, perm, info.as_dict())
+
+    def build_weighted(self, x, y, z, w, d: int, levels: int = 0, lower=(-0.5, -0.5, -0.5),
+                       upper=(0.5, 0.5, 0.5), perm=True, device_pointers: bool = False) -> BuildResult:
+        """Weighted ORB build (orb_build_weighted): uint32 weights w, reordered in place with
+        the particles."""
+        n = int(x.shape[0]) if hasattr(x, "shape") else int(x.size)
+        heap = np.zeros(2 * d - 1, CELL_DTYPE)
+        ranges = np.zeros((2 * d - 1, 2), np.uint32)
+        if perm is True:
+            perm = np.empty(n, np.uint32)
+        lo = np.asarray(lower, np.float32)
+        hi = np.asarray(upper, np.float32)
+        info = BuildInfo()
+        st = self.lib.orb_build_weighted(self.h, _ptr(x), _ptr(y), _ptr(z), _ptr(w), n, d, levels,
+                                         lo.ctypes.data, hi.ctypes.data, heap.ctypes.data,
+                                         ranges.ctypes.data, _ptr(perm),
+                                         ORB_DEVICE_POINTERS if device_pointers else 0, ctypes.byref(info))
         self._check(st)
         return BuildResult(heap, ranges, perm, info.as_dict())
 

@@ -130,6 +130,27 @@ orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uin
                      orb_build_info *info);
 
 /*
+ * Weighted build (no counterpart in the reference's code; its thesis specifies weighted ORB,
+ * documentation/notes.tex:259-271, 326-336, and the reference never implements it). Every
+ * particle carries an integer weight w[i] (work units, e.g. timesteps); the weights are
+ * reordered with their particles. A cell of k leaves looks for the cut that gives its left
+ * child the share ceil(k/2)/k of its weight W, with the reference's loop (midpoint cuts of
+ * the bracket, at most 32 sweeps, src/orbit.cpp:146-232) and its test made exact and weighted:
+ *   D = k W_left - ceil(k/2) W   (W_left: the weights of the keys below the cut)
+ *   found when D == 0 or n |D| < 3 k W (n particles: |W_left - ratio W| below 3 mean weights);
+ *   otherwise the right margin moves when D > 0, the left one when D < 0.
+ * The sums are 64-bit integers, so the result does not depend on the order of summation. With
+ * every weight 1 the test is |cl - ratio c| < 3 exactly, which is the reference's float32 test
+ * wherever that test is exact (cells below 2^24 particles, an even leaf count): the tree is
+ * then orb_build's. Arguments as orb_build, plus w: n weights (host, or device with
+ * ORB_DEVICE_POINTERS), permuted in place. Uses the level-by-level path for every level.
+ */
+orb_status orb_build_weighted(orb_ctx *ctx, float *x, float *y, float *z, uint32_t *w, uint64_t n,
+                              uint32_t d, uint32_t levels, const float lower[3],
+                              const float upper[3], orb_cell_t *heap, uint32_t *ranges,
+                              uint32_t *perm, uint32_t flags, orb_build_info *info);
+
+/*
  * Batched build (no counterpart in the reference, which builds one tree per run): k
  * independent ORB instances of uneven sizes, packed in one set of particle arrays, built
  * together level by level (every level's kernels cover the cells of all instances).

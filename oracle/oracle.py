@@ -93,6 +93,14 @@ def lib():
                                    fp, fp, ctypes.c_void_p, u32p, u32p,
                                    ctypes.POINTER(ctypes.c_uint8), ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int, ctypes.POINTER(_Stats)]
+        L.oracle_convergence_weighted.restype = ctypes.c_int
+        L.oracle_convergence_weighted.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                                  ctypes.c_int32]
+        L.oracle_build_weighted.restype = ctypes.c_int
+        L.oracle_build_weighted.argtypes = [fp, fp, fp, u32p, ctypes.c_uint64, ctypes.c_uint32,
+                                            ctypes.c_uint32, fp, fp, ctypes.c_void_p, u32p, u32p,
+                                            ctypes.POINTER(ctypes.c_uint8), ctypes.c_int,
+                                            ctypes.POINTER(_Stats)]
         L.oracle_level_shape.restype = None
         L.oracle_level_shape.argtypes = [ctypes.c_uint32, u32p, u32p]
         L.oracle_max_levels.restype = ctypes.c_uint32
@@ -227,3 +235,35 @@ def cut_of(heap: np.ndarray) -> np.ndarray:
     """getCut() of every heap cell, float32 exactly as src/cell.h:74-76 computes it."""
     s = (heap["cutMarginRight"] + heap["cutMarginLeft"]).astype(np.float32)
     return (s.astype(np.float64) / 2.0).astype(np.float32)
+
+
+def convergence_weighted(w_left: int, w_cell: int, n: int, n_leaf: int) -> int:
+    """The weighted test: 0 found, +1 right margin moves, -1 left (see orb_oracle.h)."""
+    return int(lib().oracle_convergence_weighted(w_left, w_cell, n, n_leaf))
+
+
+def build_tree_weighted(x, y, z, w, d: int, levels: int | None = None, lower=(-0.5, -0.5, -0.5),
+                        upper=(0.5, 0.5, 0.5), threads: int = 1):
+    """Weighted ORB build (uint32 weights, permuted with the particles). Returns
+    (OracleResult, permuted weights)."""
+    x, y, z = (np.array(a, dtype=np.float32, copy=True) for a in (x, y, z))
+    w = np.array(w, dtype=np.uint32, copy=True)
+    n = x.size
+    levels = max_levels(d) if levels is None else levels
+    heap = np.zeros(2 * d - 1, CELL_DTYPE)
+    ranges = np.zeros((1, 2 * d - 1, 2), np.uint32)
+    perm = np.empty(n, np.uint32)
+    iters = np.zeros(2 * d - 1, np.uint8)
+    lo = np.asarray(lower, np.float32)
+    hi = np.asarray(upper, np.float32)
+    st = _Stats()
+    rc = lib().oracle_build_weighted(_f(x), _f(y), _f(z), _u32(w), n, d, levels, _f(lo), _f(hi),
+                                     heap.ctypes.data_as(ctypes.c_void_p), _u32(ranges), _u32(perm),
+                                     iters.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), threads,
+                                     ctypes.byref(st))
+    if rc != 0:
+        raise ValueError(f"oracle_build_weighted rejected the arguments (code {rc})")
+    stats = {"levels_built": st.levels_built, "iterations": list(st.iterations[: st.levels_built]),
+             "degenerate_cells": st.degenerate_cells, "zero_volume_cells": st.zero_volume_cells,
+             "unfound_cells": st.unfound_cells}
+    return OracleResult(x, y, z, heap, ranges, perm, iters, stats), w

@@ -137,22 +137,48 @@ int convergence(uint32_t count_left, uint32_t count, int32_t n_leaf, int32_t *di
     return difference > 0 ? 1 : -1;
 }
 
+// Weighted ORB (documentation/notes.tex:259-271, 326-336: the left cell gets the share
+// ceil(k/2)/k of the cell's weight; never implemented by the reference). Weights are
+// integers, so the sums are exact in any order. The test is the reference's
+// |W_left - ratio W| < 3 (src/orbit.cpp:204-208) with the tolerance scaled by the cell's
+// mean weight W/n and evaluated exactly in 128-bit integers:
+//   D = k W_left - ceil(k/2) W;  found when D == 0 or n |D| < 3 k W;  else the right margin
+//   moves for D > 0 and the left one for D < 0.
+// With every weight 1 this is |cl - ratio c| < 3 exactly: the reference's float32 test
+// whenever that test is exact (counts below 2^24, an even k).
+int convergence_weighted(uint64_t w_left, uint64_t w_cell, uint64_t n, int32_t n_leaf) {
+    const __int128 k = n_leaf, half = (n_leaf + 1) / 2;
+    const __int128 D = k * (__int128)w_left - half * (__int128)w_cell;
+    const unsigned __int128 ad = (unsigned __int128)(D < 0 ? -D : D);
+    if (D == 0 || (unsigned __int128)n * ad < (unsigned __int128)3 * (unsigned __int128)k * w_cell) return 0;
+    return D > 0 ? 1 : -1;
+}
+
+uint64_t weight_left(const float *keys, const uint32_t *w, uint64_t begin, uint64_t end, float cut) {
+    uint64_t s = 0;
+    for (uint64_t p = begin; p < end; ++p) s += keys[p] < cut ? w[p] : 0u;
+    return s;
+}
+
 uint32_t count_left(const float *keys, uint64_t begin, uint64_t end, float cut) {  // countLeft.cpp:31-36
     uint32_t n_left = 0;
     for (const float *p = keys + begin, *e = keys + end; p < e; ++p) n_left += *p < cut;
     return n_left;
 }
 
-inline void swap3(float *x, float *y, float *z, uint32_t *perm, int64_t a, int64_t b) {
+inline void swap3(float *x, float *y, float *z, uint32_t *perm, int64_t a, int64_t b,
+                  uint32_t *wt = nullptr) {
     std::swap(x[a], x[b]);
     std::swap(y[a], y[b]);
     std::swap(z[a], z[b]);
     if (perm) std::swap(perm[a], perm[b]);
+    if (wt) std::swap(wt[a], wt[b]);
 }
 
-// partition.cpp:30-52 with the scan clamped at the cell end.
+// partition.cpp:30-52 with the scan clamped at the cell end (weights, if any, move with
+// their particles).
 int64_t hoare(float *x, float *y, float *z, uint32_t *perm, int64_t begin, int64_t end,
-              int axis, float cut, bool final_swap, int *degenerate) {
+              int axis, float cut, bool final_swap, int *degenerate, uint32_t *wt = nullptr) {
     float *key = axis == 0 ? x : (axis == 1 ? y : z);
     int64_t i = begin - 1, j = end;
     for (;;) {
@@ -163,10 +189,10 @@ int64_t hoare(float *x, float *y, float *z, uint32_t *perm, int64_t begin, int64
             --j;
         } while (j >= begin && key[j] > cut);
         if (i >= j) break;
-        swap3(x, y, z, perm, i, j);
+        swap3(x, y, z, perm, i, j, wt);
     }
     if (i < end) {
-        if (final_swap) swap3(x, y, z, perm, i, end - 1);
+        if (final_swap) swap3(x, y, z, perm, i, end - 1, wt);
         if (degenerate) *degenerate = 0;
     } else {
         i = end;
@@ -602,6 +628,112 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
         st.levels_built = l;
     }
     st.degenerate_cells = degen[0];
+    st.t_total_s = now_s() - t0;
+    if (stats) *stats = st;
+    return 0;
+}
+
+int oracle_convergence_weighted(uint64_t w_left, uint64_t w_cell, uint64_t n, int32_t n_leaf) {
+    return convergence_weighted(w_left, w_cell, n, n_leaf);
+}
+
+int oracle_build_weighted(float *x, float *y, float *z, uint32_t *w, uint64_t n, uint32_t d,
+                          uint32_t levels, const float lower[3], const float upper[3],
+                          oracle_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint8_t *iters,
+                          int threads, oracle_stats_t *stats) {
+    if (!x || !y || !z || !w || !heap || !ranges || d == 0 || d > (1u << 30)) return -1;
+    if (n >= (1ull << 31)) return -2;
+    if (levels > oracle_max_levels(d) || levels >= ORACLE_MAX_LEVELS) return -3;
+    if (threads < 1) threads = 1;
+    uint32_t depth, last_cells;
+    oracle_level_shape(d, &depth, &last_cells);
+    oracle_stats_t st;
+    std::memset(&st, 0, sizeof st);
+    st.nranks = 1;
+    const double t0 = now_s();
+    const uint64_t heap_size = 2ull * d - 1;
+    std::memset(heap, 0, heap_size * sizeof(Cell));
+    std::memset(ranges, 0, heap_size * 2 * sizeof(uint32_t));
+    if (iters) std::memset(iters, 0, heap_size);
+    if (perm)
+        for (uint64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+    Cell root = make_cell(0, (int)d, lower, upper);  // orbit.cpp:74-81
+    root.cutAxis = 0;
+    set_cut_margin(root);
+    heap[0] = root;
+    ranges[0] = 0;
+    ranges[1] = (uint32_t)n;
+    RankPool pool(threads);
+    std::atomic<uint32_t> degen(0), unfound(0);
+    const float *axes[3] = {x, y, z};
+    for (uint32_t l = 1; l <= levels; ++l) {
+        const int a = (1 << (l - 1)) - 1;
+        const int b = std::min<int>((int)last_cells, 1 << l) - 2;
+        const int n_cells = b - a + 1;
+        if (n_cells <= 0) {
+            st.levels_built = l;
+            continue;
+        }
+        Cell *cells = heap + a;
+        std::vector<uint32_t> jdone(n_cells, 0);
+        std::atomic<int> next(0);
+        // the loop of orbit.cpp:146-232 per cell (independent of the other cells), with the
+        // weight sums in place of the counts
+        pool.run([&](int) {
+            for (int c; (c = next.fetch_add(1)) < n_cells;) {
+                Cell &cell = cells[c];
+                const uint32_t bg = ranges[2 * cell.id], en = ranges[2 * cell.id + 1];
+                uint64_t w_cell = 0;
+                for (uint32_t p = bg; p < en; ++p) w_cell += w[p];
+                int j = 0;
+                while (!cell.foundCut && j < 32) {
+                    ++j;
+                    const uint64_t wl = weight_left(axes[eff_axis(cell)], w, bg, en, get_cut(cell));
+                    const int dir = convergence_weighted(wl, w_cell, en - bg, cell.nLeafCells);
+                    if (dir == 0)
+                        cell.foundCut = 1;
+                    else if (dir > 0)
+                        cell.cutMarginRight = get_cut(cell);
+                    else
+                        cell.cutMarginLeft = get_cut(cell);
+                }
+                if (iters) iters[cell.id] = (uint8_t)j;
+                jdone[c] = (uint32_t)j;
+                if (!cell.foundCut) ++unfound;
+            }
+        });
+        uint32_t jmax = 0;
+        for (int c = 0; c < n_cells; ++c) {
+            jmax = std::max(jmax, jdone[c]);
+            st.cell_counts += jdone[c];
+        }
+        st.iterations[l - 1] = jmax;
+        for (int c = 0; c < n_cells; ++c) {  // orbit.cpp:235-250
+            Cell lc, rc;
+            split(cells[c], lc, rc, &st.zero_volume_cells);
+            heap[lc.id] = lc;
+            heap[rc.id] = rc;
+        }
+        next = 0;
+        pool.run([&](int) {  // partition.cpp:18-62, weights moving with their particles
+            for (int c; (c = next.fetch_add(1)) < n_cells;) {
+                const Cell &cell = cells[c];
+                const uint32_t bg = ranges[2 * cell.id], en = ranges[2 * cell.id + 1];
+                int dg = 0;
+                const int64_t i = hoare(x, y, z, perm, bg, en, eff_axis(cell), get_cut(cell), true,
+                                        &dg, w);
+                degen += (uint32_t)dg;
+                const int lcid = 2 * cell.id + 1, rcid = 2 * cell.id + 2;
+                ranges[2 * lcid] = bg;
+                ranges[2 * lcid + 1] = (uint32_t)i;
+                ranges[2 * rcid] = (uint32_t)i;
+                ranges[2 * rcid + 1] = en;
+            }
+        });
+        st.levels_built = l;
+    }
+    st.degenerate_cells = degen;
+    st.unfound_cells = unfound;
     st.t_total_s = now_s() - t0;
     if (stats) *stats = st;
     return 0;

@@ -111,6 +111,25 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
                  uint32_t *ranges, uint32_t *perm, uint8_t *iters, int nranks,
                  int make_axis, int threads, oracle_stats_t *stats);
 
+/*
+ * Weighted ORB (documentation/notes.tex:259-271, 326-336; the reference never implemented
+ * it): each particle carries an integer weight w[i] (work units), permuted with it. A cell's
+ * bisection looks for the cut that gives its left child the share ceil(k/2)/k of the cell's
+ * weight W (k leaves), with the reference's loop (src/orbit.cpp:146-232: midpoint cuts, at
+ * most 32 sweeps) and its test made exact and weighted (oracle_convergence_weighted):
+ *   D = k W_left - ceil(k/2) W; found when D == 0 or n |D| < 3 k W (n particles); the right
+ *   margin moves for D > 0, the left one for D < 0.
+ * W_left is the integer sum of the weights of the keys below the cut. With unit weights the
+ * test is |cl - c ratio| < 3 exactly, the reference's float32 test wherever that is exact
+ * (cells below 2^24 particles, even k): the tree is then the unweighted one.
+ * Single rank; threads as in oracle_build. Same outputs as oracle_build, w permuted too.
+ */
+int oracle_convergence_weighted(uint64_t w_left, uint64_t w_cell, uint64_t n, int32_t n_leaf);
+int oracle_build_weighted(float *x, float *y, float *z, uint32_t *w, uint64_t n, uint32_t d,
+                          uint32_t levels, const float lower[3], const float upper[3],
+                          oracle_cell_t *heap, uint32_t *ranges, uint32_t *perm, uint8_t *iters,
+                          int threads, oracle_stats_t *stats);
+
 /* Cell::getNLevels() (depth = ceil(log2 d)) and getNCellsOnLastLevel() (2d - 2^depth) of
  * src/cell.h:65-72. */
 void oracle_level_shape(uint32_t d, uint32_t *depth, uint32_t *last);

@@ -412,3 +412,28 @@ def test_engine_leaf_ratio_is_the_references(tmp_path):
     assert out.returncode == 0, out.stdout
     cnt, bad = (int(v) for v in out.stdout.split())
     assert bad == 0 and cnt > 8_000_000
+
+
+def test_weighted_oracle(oracle):
+    """Weighted ORB: unit weights give the unweighted tree (cells below 2^24, d a power of
+    two), weights move with their particles, the exact test's edges."""
+    n, d = 1 << 16, 1 << 7
+    x, y, z = oracle.gen_plummer(8, n)
+    plain = oracle.build_tree(x, y, z, d)
+    unit, w1 = oracle.build_tree_weighted(x, y, z, np.ones(n, np.uint32), d)
+    assert unit.heap.tobytes() == plain.heap.tobytes() and np.array_equal(unit.perm, plain.perm)
+    w = np.random.default_rng(1).integers(1, 100, n).astype(np.uint32)
+    r, wp = oracle.build_tree_weighted(x, y, z, w, d, threads=4)
+    assert np.array_equal(wp, w[r.perm])
+    leaves = r.ranges[0][d - 1:]
+    sums = np.array([int(wp[b:e].sum()) for b, e in leaves])
+    assert sums.max() - sums.min() < 0.05 * sums.mean()
+    # the test: |W_left - ratio W| < 3 W / n, D == 0 always found
+    assert oracle.convergence_weighted(50, 100, 100, 2) == 0
+    assert oracle.convergence_weighted(52, 100, 100, 2) == 0       # |52 - 50| < 3
+    assert oracle.convergence_weighted(53, 100, 100, 2) == 1
+    assert oracle.convergence_weighted(0, 0, 0, 2) == 0             # empty cell
+    # k = 3 leaves, W = 300 over n = 100: target 2/3 W = 200, tolerance 3 x mean weight = 9
+    assert oracle.convergence_weighted(212, 300, 100, 3) == 1
+    assert oracle.convergence_weighted(208, 300, 100, 3) == 0
+    assert oracle.convergence_weighted(190, 300, 100, 3) == -1
