@@ -98,6 +98,7 @@ struct orb_ctx {
     DevBuf<uint8_t> warm;
     DevBuf<uint32_t> sub_flag;  // subtree path taken (one word)
     DevBuf<uint32_t> w;         // weighted builds from host memory: the weights
+    DevBuf<unsigned long long> gen_starts;  // xorshf96 generator: chunk start states
     DevBuf<unsigned long long> whist, wbelow, wtot;  // weighted builds: per-cell weight sums
     BuildCounters *h_counters = nullptr;  // pinned
     uint32_t *h_sub_flag = nullptr;       // pinned: the subtree path was taken
@@ -688,6 +689,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     }
     ctx->hint.release(); ctx->hint_axis.release(); ctx->warm.release(); ctx->sub_flag.release();
     ctx->w.release(); ctx->whist.release(); ctx->wbelow.release(); ctx->wtot.release();
+    ctx->gen_starts.release();
     ctx->listed.release(); ctx->cmp_bad.release(); ctx->cmp_off.release(); ctx->cmp_cnt.release();
     ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -909,11 +911,61 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
     return ORB_OK;
 }
 
+// The reference's xorshf96 (src/services/init.cu:11-25) is a linear map of its 192-bit state
+// over GF(2): s -> M s. Its stream is cut into chunks of kXsChunk draws; the start of chunk g
+// is M^(offset + g kXsChunk) s0, by a matrix power (squaring) and one product per chunk.
+namespace xs96 {
+struct State {
+    unsigned long long w[3];
+};
+inline void step(State &s) {
+    unsigned long long x = s.w[0];
+    x ^= x << 16;
+    x ^= x >> 5;
+    x ^= x << 1;
+    const unsigned long long t = x;
+    s.w[0] = s.w[1];
+    s.w[1] = s.w[2];
+    s.w[2] = t ^ s.w[0] ^ s.w[1];
+}
+struct Mat {
+    State col[192];  // column j: the image of state bit j
+};
+inline State apply(const Mat &m, const State &v) {
+    State r = {{0, 0, 0}};
+    for (int j = 0; j < 192; ++j)
+        if ((v.w[j >> 6] >> (j & 63)) & 1ull)
+            for (int k = 0; k < 3; ++k) r.w[k] ^= m.col[j].w[k];
+    return r;
+}
+inline Mat mul(const Mat &a, const Mat &b) {  // a b
+    Mat c;
+    for (int j = 0; j < 192; ++j) c.col[j] = apply(a, b.col[j]);
+    return c;
+}
+inline Mat power(uint64_t k) {  // M^k
+    Mat base, acc;
+    for (int j = 0; j < 192; ++j) {
+        State e = {{0, 0, 0}};
+        e.w[j >> 6] = 1ull << (j & 63);
+        acc.col[j] = e;
+        step(e);
+        base.col[j] = e;
+    }
+    for (; k; k >>= 1) {
+        if (k & 1) acc = mul(acc, base);
+        base = mul(base, base);
+    }
+    return acc;
+}
+constexpr uint32_t kXsChunk = 4096;
+}  // namespace xs96
+
 orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float *x, float *y,
                         float *z, uint32_t flags) {
     if (!ctx) return ORB_ERR_INVALID_ARGUMENT;
     ctx->err.clear();
-    if (kind != ORB_GEN_UNIFORM && kind != ORB_GEN_PLUMMER)
+    if (kind != ORB_GEN_UNIFORM && kind != ORB_GEN_PLUMMER && kind != ORB_GEN_XORSHF96)
         return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "unknown generator kind");
     if (n == 0) return ORB_OK;
     if (!x || !y || !z) return fail(ctx, ORB_ERR_INVALID_ARGUMENT, "null pointer");
@@ -929,7 +981,32 @@ orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float
         dz = ctx->z.p;
     }
     ctx->launches[kKGenerate] += 1;
-    if (kind == ORB_GEN_UNIFORM) {
+    if (kind == ORB_GEN_XORSHF96) {
+        // chunk starts: M^seed s0 (seed = draws to skip), then one jump of kXsChunk per chunk
+        static std::mutex mu;
+        static bool have = false;
+        static xs96::Mat jump;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (!have) {
+                jump = xs96::power(xs96::kXsChunk);
+                have = true;
+            }
+        }
+        const uint64_t draws = 3 * n, chunks = (draws + xs96::kXsChunk - 1) / xs96::kXsChunk;
+        std::vector<unsigned long long> starts(3 * chunks);
+        xs96::State s0 = {{123456789ull, 362436069ull, 521288629ull}};  // init.cu:11
+        if (seed) s0 = xs96::apply(xs96::power(seed), s0);
+        for (uint64_t g = 0; g < chunks; ++g) {
+            for (int k = 0; k < 3; ++k) starts[3 * g + k] = s0.w[k];
+            s0 = xs96::apply(jump, s0);
+        }
+        ORB_CUDA(ctx->gen_starts.ensure(starts.size()));
+        ORB_CUDA(cudaMemcpyAsync(ctx->gen_starts.p, starts.data(), starts.size() * sizeof(unsigned long long),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+        launch_gen_xorshf96(ctx->gen_starts.p, draws, xs96::kXsChunk, dx, dy, dz, ctx->stream);
+        ORB_CUDA(cudaStreamSynchronize(ctx->stream));  // `starts` goes out of scope
+    } else if (kind == ORB_GEN_UNIFORM) {
         launch_gen_uniform(seed, n, dx, dy, dz, ctx->stream);
     } else {
         // Cluster table, computed on the host exactly as the CPU oracle computes it.

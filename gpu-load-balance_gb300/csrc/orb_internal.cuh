@@ -276,6 +276,9 @@ void launch_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n, 
 cudaError_t configure_kernels();  // once per device (dynamic shared memory limits)
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);
+// `draws` draws of the reference's xorshf96 stream, thread g from starts[3g..3g+2] for `chunk`
+void launch_gen_xorshf96(const unsigned long long *starts, uint64_t draws, uint32_t chunk,
+                         float *x, float *y, float *z, cudaStream_t st);
 void launch_gen_plummer(uint64_t seed, uint64_t n, const float *centres, const double *scales,
                         float *x, float *y, float *z, cudaStream_t st);
 

@@ -3048,6 +3048,32 @@ __global__ void k_gen_plummer(uint64_t seed, uint64_t n, PlummerTable tab, float
     }
 }
 
+// The reference's xorshf96 stream (src/services/init.cu:11-25): thread g continues the
+// stream from starts[g] (its state after g * chunk draws, computed on the host by a GF(2)
+// jump) for `chunk` draws; draw j is coordinate j % 3 of particle j / 3. Value:
+// (float)z / 2^64 - 0.5 (exact scaling, then the subtraction rounded once: the reference's
+// double subtraction rounded to float gives the same float).
+__global__ void k_gen_xorshf96(const unsigned long long *starts, uint64_t draws, uint32_t chunk,
+                               float *x, float *y, float *z) {
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t j0 = g * chunk;
+    if (j0 >= draws) return;
+    unsigned long long sx = starts[3 * g], sy = starts[3 * g + 1], sz = starts[3 * g + 2];
+    const uint64_t j1 = min(draws, j0 + chunk);
+    float *dst[3] = {x, y, z};
+    for (uint64_t j = j0; j < j1; ++j) {
+        sx ^= sx << 16;
+        sx ^= sx >> 5;
+        sx ^= sx << 1;
+        const unsigned long long t = sx;
+        sx = sy;
+        sy = sz;
+        sz = t ^ sx ^ sy;
+        const float q = __fmul_rn(__ull2float_rn(sz), 0x1p-64f);
+        dst[j % 3][j / 3] = __fsub_rn(q, 0.5f);
+    }
+}
+
 __global__ void k_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *roots, int k) {
     for (int i = blockIdx.y; i < k; i += gridDim.y) {
         const BatchRoot r = roots[i];
@@ -3193,6 +3219,12 @@ void launch_iota_u32(uint32_t *dst, uint64_t n, cudaStream_t st) {
 void launch_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
                        uint64_t n, cudaStream_t st) {
     if (n) k_gather_u32<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, src, perm, off, n);
+}
+
+void launch_gen_xorshf96(const unsigned long long *starts, uint64_t draws, uint32_t chunk,
+                         float *x, float *y, float *z, cudaStream_t st) {
+    const uint64_t threads = (draws + chunk - 1) / chunk;
+    k_gen_xorshf96<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(starts, draws, chunk, x, y, z);
 }
 
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,

@@ -47,6 +47,7 @@ assert CELL_DTYPE.itemsize == 52
 ORB_DEVICE_POINTERS = 0x1
 ORB_GEN_UNIFORM = 0
 ORB_GEN_PLUMMER = 1
+ORB_GEN_XORSHF96 = 2
 
 STATUS = {
     0: "ok",

@@ -335,16 +335,21 @@ orb_status orb_get_ranges(orb_ctx *ctx, uint32_t *ranges, uint32_t n_cells);
 orb_status orb_set_ranges(orb_ctx *ctx, const uint32_t *ranges, uint32_t n_cells);
 
 /*
- * Seeded synthetic particles (the engine's own generator; the reference's xorshf96 input,
- * src/services/init.cu:11-25, is replaced by a counter-based generator so every size and
- * seed is reproducible).
+ * Seeded synthetic particles: the engine's counter-based generators (every size and seed
+ * reproducible) and the reference's own input stream.
  *   kind ORB_GEN_UNIFORM: i.i.d. on the 2^-24 grid of [-0.5,0.5)^3
  *   kind ORB_GEN_PLUMMER: 90% from 64 Plummer spheres (scale radii log-uniform in
  *                         [0.005,0.05)), 10% uniform background, clipped to the box
+ *   kind ORB_GEN_XORSHF96: the reference's xorshf96 (ServiceInit, src/services/init.cu:11-25,
+ *                         48-52): from its process-start seeds, x_0, y_0, z_0, x_1, ... each
+ *                         (float)z / ULONG_MAX - 0.5 in [-0.5, 0.5]; `seed` = draws of the
+ *                         stream to skip first (0: the input of a single-rank `orbit N d 0`).
+ *                         Generated on the device by jumps of the generator's linear map.
  * Writes n floats to each of x,y,z (device pointers if ORB_DEVICE_POINTERS, else host).
  */
 #define ORB_GEN_UNIFORM 0
 #define ORB_GEN_PLUMMER 1
+#define ORB_GEN_XORSHF96 2
 orb_status orb_generate(orb_ctx *ctx, int kind, uint64_t seed, uint64_t n, float *x, float *y,
                         float *z, uint32_t flags);
 

@@ -75,6 +75,8 @@ def lib():
             f = getattr(L, name)
             f.restype = None
             f.argtypes = [ctypes.c_uint64, ctypes.c_uint64, fp, fp, fp, ctypes.c_int]
+        L.oracle_gen_xorshf96.restype = None
+        L.oracle_gen_xorshf96.argtypes = [ctypes.c_uint64, fp, fp, fp]
         L.oracle_plummer_clusters.restype = None
         L.oracle_plummer_clusters.argtypes = [ctypes.c_uint64, fp, ctypes.POINTER(ctypes.c_double)]
         L.oracle_get_cut.restype = ctypes.c_float
@@ -130,6 +132,13 @@ def gen_uniform(seed: int, n: int, nthreads: int = 8):
 def gen_plummer(seed: int, n: int, nthreads: int = 8):
     x, y, z = (np.empty(n, np.float32) for _ in range(3))
     lib().oracle_gen_plummer(seed, n, _f(x), _f(y), _f(z), nthreads)
+    return x, y, z
+
+
+def gen_xorshf96(n: int):
+    """The reference's own input stream (src/services/init.cu:11-25), n particles."""
+    x, y, z = (np.empty(n, np.float32) for _ in range(3))
+    lib().oracle_gen_xorshf96(n, _f(x), _f(y), _f(z))
     return x, y, z
 
 

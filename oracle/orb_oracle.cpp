@@ -339,6 +339,32 @@ void oracle_gen_plummer(uint64_t seed, uint64_t n, float *x, float *y, float *z,
     });
 }
 
+// The reference's generator, src/services/init.cu:11-25: three 64-bit words (unsigned long on
+// its LP64 targets) from the seeds 123456789, 362436069, 521288629 at process start, one
+// xorshift step per draw, the value (float)z / ULONG_MAX - 0.5 (the division in float by
+// the float nearest ULONG_MAX, 2^64; the subtraction in double, then rounded to float), and
+// particles(i, d) filled for i = 0.., d = 0, 1, 2 (init.cu:48-52): the single-rank input of
+// `orbit N d 0`.
+void oracle_gen_xorshf96(uint64_t n, float *x, float *y, float *z) {
+    uint64_t sx = 123456789, sy = 362436069, sz = 521288629;
+    auto draw = [&]() -> float {
+        uint64_t t;
+        sx ^= sx << 16;
+        sx ^= sx >> 5;
+        sx ^= sx << 1;
+        t = sx;
+        sx = sy;
+        sy = sz;
+        sz = t ^ sx ^ sy;
+        return (float)sz / (float)UINT64_MAX - 0.5;
+    };
+    for (uint64_t i = 0; i < n; ++i) {
+        x[i] = draw();
+        y[i] = draw();
+        z[i] = draw();
+    }
+}
+
 float oracle_get_cut(float margin_left, float margin_right) {
     Cell c;
     c.cutMarginLeft = margin_left;

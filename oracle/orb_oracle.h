@@ -71,6 +71,10 @@ void oracle_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
 void oracle_plummer_clusters(uint64_t seed, float *centres /*64*3*/, double *scales /*64*/);
 void oracle_gen_plummer(uint64_t seed, uint64_t n, float *x, float *y, float *z, int nthreads);
 
+/* The reference's own generator (src/services/init.cu:11-25), the stream a single-rank
+ * `orbit N d 0` builds from: x_0, y_0, z_0, x_1, ... from the process-start seeds. */
+void oracle_gen_xorshf96(uint64_t n, float *x, float *y, float *z);
+
 /* Reference arithmetic primitives. */
 float oracle_get_cut(float margin_left, float margin_right);
 /* Returns 0 = found, +1 = move the right margin to the cut, -1 = move the left margin. */

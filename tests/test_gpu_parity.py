@@ -46,6 +46,29 @@ def test_generator_bit_exact(ctx, engine, oracle, kind):
     assert np.array_equal(gx, x) and np.array_equal(gy, y) and np.array_equal(gz, z)
 
 
+def test_reference_generator_stream(ctx, engine, oracle):
+    """ORB_GEN_XORSHF96: the reference's own input stream (src/services/init.cu:11-25),
+    generated on the device by jumps of the generator's linear map, bit for bit the
+    sequential stream; `seed` skips draws."""
+    n = (1 << 20) + 7
+    x, y, z = oracle.gen_xorshf96(n)
+    gx, gy, gz = ctx.generate_host(engine.ORB_GEN_XORSHF96, 0, n)
+    assert np.array_equal(gx, x) and np.array_equal(gy, y) and np.array_equal(gz, z)
+    k = 12345
+    sx, sy, sz = ctx.generate_host(engine.ORB_GEN_XORSHF96, 3 * k, n - k)
+    assert np.array_equal(sx, x[k:]) and np.array_equal(sz, z[k:])
+    sx, sy, sz = ctx.generate_host(engine.ORB_GEN_XORSHF96, 1, 5)  # skip one draw: y_0 first
+    assert sx[0] == y[0] and sy[0] == z[0] and sz[0] == x[1]
+
+
+def test_reference_input_build(ctx, engine, oracle):
+    """`orbit 20 10 0` on the reference's own input: 2^20 xorshf96 particles, 2^10 leaves,
+    the reference's loop bound (9 levels), bit-exact."""
+    n, d = 1 << 20, 1 << 10
+    x, y, z = ctx.generate_host(engine.ORB_GEN_XORSHF96, 0, n)
+    run_both(ctx, oracle, x, y, z, d, levels=9)
+
+
 @pytest.mark.parametrize("n,d,seed", [(1 << 12, 1 << 4, 1), (1 << 16, 1 << 8, 2),
                                       ((1 << 16) + 123, 1 << 9, 3), (50000, 1 << 12, 4)])
 def test_uniform_parity(any_ctx, oracle, n, d, seed):
