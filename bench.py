@@ -18,6 +18,8 @@ by a device-to-device restore of the unpartitioned input (the build partitions i
              leg runs the single-rank oracle on the benchmark's own inputs (outside every
              timed region) as the checker of the GPU outputs: "parity"
   clustered  the same measurements for 2^26 Plummer-clustered particles into 2^18 leaves
+  weighted   weighted ORB (integer weights per particle, a labelled mode) on 2^26 clustered
+             particles into 2^16 leaves
   batched    128 uneven instances in one batched build against one build at a time
   served     a Poisson request stream through the continuous-batching server
 
@@ -49,6 +51,7 @@ WARM_WIDTH = 8.0  # warm rebuild: bracket factor (half-width = factor x extent /
 UNIT = "particles/s"
 FALLBACK_HBM_GBS = 6800.0
 CLUSTERED = (1 << 26, 1 << 18)
+WEIGHTED = (1 << 26, 1 << 16)
 TRAFFIC_PROFILE = "dram_traffic_part_swap_hist_classify_subtree_2p24_2p13.txt"
 # every kernel kind that counts keys below a cut (the count-left family)
 COUNT_LEFT_KERNELS = ("count_left_hist", "bisect_tile", "bisect_cta", "count_left_sample",
@@ -235,16 +238,23 @@ def check_parity(job):
     out = {"oracle": "single-rank restatement of the reference's CPU path, run on the "
                      "benchmark's own inputs", "compared": ["heap", "ranges", "perm", "x", "y", "z"]}
     ok, cells, particles = True, 0, 0
+    weighted = "w" in job
+    if weighted:
+        out["compared"].append("w")
     for inst in job["instances"]:
-        x, y, z = (job["x"][inst["offset"]:inst["offset"] + inst["n"]],
-                   job["y"][inst["offset"]:inst["offset"] + inst["n"]],
-                   job["z"][inst["offset"]:inst["offset"] + inst["n"]])
-        ref = O.build_tree(x, y, z, inst["d"], threads=threads)
-        heap, ranges, gx, gy, gz, perm = inst["gpu"]
+        sl = slice(inst["offset"], inst["offset"] + inst["n"])
+        x, y, z = job["x"][sl], job["y"][sl], job["z"][sl]
+        if weighted:
+            ref, wref = O.build_tree_weighted(x, y, z, job["w"][sl], inst["d"], threads=threads)
+        else:
+            ref = O.build_tree(x, y, z, inst["d"], threads=threads)
+        heap, ranges, gx, gy, gz, perm = inst["gpu"][:6]
         same = (heap.tobytes() == ref.heap.tobytes() and np.array_equal(ranges, ref.ranges[0])
                 and np.array_equal(perm, ref.perm)
                 and all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
                         for a, b in ((gx, ref.x), (gy, ref.y), (gz, ref.z))))
+        if weighted:
+            same = same and np.array_equal(inst["gpu"][6], wref)
         ok = ok and same
         cells += len(ref.heap)
         particles += inst["n"]
@@ -520,6 +530,64 @@ def run_plain(ctx, E, torch, dev, args, kind: str, n: int, d: int, seed: int, pe
 
 
 # ------------------------------------------------------------------------------------------
+# Weighted ORB: integer weights per particle (orb_build_weighted), a labelled mode
+# ------------------------------------------------------------------------------------------
+def bench_weighted(ctx, E, torch, dev, args, n: int, d: int, seed: int, peak: float):
+    import numpy as np
+
+    x0, y0, z0 = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    ctx.generate(E.ORB_GEN_PLUMMER, seed, n, x0, y0, z0, device_pointers=True)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    w0 = torch.randint(1, 64, (n,), generator=g, device=dev, dtype=torch.int32)
+    x, y, z, w = (torch.empty_like(a) for a in (x0, y0, z0, w0))
+    perm = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def step(with_perm=False):
+        for dst, src in ((x, x0), (y, y0), (z, z0), (w, w0)):
+            dst.copy_(src)
+        torch.cuda.synchronize(dev)
+        return ctx.build_weighted(x, y, z, w, d, perm=perm if with_perm else None,
+                                  device_pointers=True)
+
+    ctx.profile_reset(timing=True)
+    for _ in range(max(args.warmup, 1)):
+        step()
+    prof = ctx.profile()
+    ms = []
+    for _ in range(args.steps):
+        ms.append(step().info["device_ms"])
+    res = step(with_perm=True)
+    wsteps = max(args.warmup, 1)
+    wh = prof.get("count_left_weighted", {"bytes": 0.0, "total_ms": 0.0})
+    gbs = wh["bytes"] / (wh["total_ms"] / 1e3) / 1e9 if wh["total_ms"] else None
+    gpu = (res.heap.copy(), res.ranges.copy(), x.cpu().numpy(), y.cpu().numpy(), z.cpu().numpy(),
+           perm.cpu().numpy().view(np.uint32), w.cpu().numpy().view(np.uint32))
+    job = {"x": x0.cpu().numpy(), "y": y0.cpu().numpy(), "z": z0.cpu().numpy(),
+           "w": w0.cpu().numpy().view(np.uint32),
+           "instances": [{"offset": 0, "n": n, "d": d, "gpu": gpu}]}
+    kernels = {k: {"launches": v["launches"] // wsteps, "ms": round(v["total_ms"] / wsteps, 4)}
+               for k, v in prof.items()}
+    del x0, y0, z0, w0, x, y, z, w, perm
+    torch.cuda.empty_cache()
+    leaves = res.ranges[d - 1:]
+    wp = gpu[6]
+    sums = np.array([int(wp[b:e].sum()) for b, e in leaves], dtype=np.float64)
+    return {
+        "workload": f"{workload_name('plummer', n, d)}, integer weights uniform in 1..63 per particle",
+        "build_ms_device": round(statistics.median(ms), 4),
+        "particles_per_s": n / (statistics.median(ms) / 1e3),
+        "count_left_weighted": {"achieved": round(gbs, 1) if gbs else None, "unit": "GB/s",
+                                "frac": round(gbs / peak, 4) if gbs else None,
+                                "bytes": "8 B per key and pass (key + weight)"},
+        "leaf_weight_spread": round(float((sums.max() - sums.min()) / sums.mean()), 5),
+        "kernels_per_step_warmup": kernels,
+        "note": "labelled mode (the reference never implemented weighted ORB): every level "
+                "through the weighted passes, no subtree kernel",
+    }, job
+
+
+# ------------------------------------------------------------------------------------------
 # Batched workload: 128 uneven instances, batched build vs one instance at a time
 # ------------------------------------------------------------------------------------------
 def bench_batched(ctx, E, torch, dev, steps: int, warmup: int, seed: int):
@@ -738,6 +806,9 @@ def gpu_arm(args):
         cl = run_plain(ctx, E, torch, dev, args, "plummer", cn, cd, SEED + 33, peak, peak_kind, None)
         jobs["clustered"] = cl.pop("parity_job")
         clustered = cl
+    weighted = None
+    if not args.no_weighted:
+        weighted, jobs["weighted"] = bench_weighted(ctx, E, torch, dev, args, *WEIGHTED, SEED + 55, peak)
     batched = None
     if not args.no_batched:
         batched, jobs["batched"] = bench_batched(ctx, E, torch, dev, max(2, min(args.steps, 5)), 1,
@@ -761,6 +832,8 @@ def gpu_arm(args):
         clustered = _section(clustered, parity.get("clustered"))
     if batched is not None:
         batched["parity"] = parity.get("batched")
+    if weighted is not None:
+        weighted["parity"] = parity.get("weighted")
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -784,6 +857,7 @@ def gpu_arm(args):
         "gpu_launches": head["launches"],
         "cpu_baseline": cpu,
         "clustered": clustered,
+        "weighted": weighted,
         "batched": batched,
         "served": served,
         "clocks": clock_summary,
@@ -809,6 +883,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-clustered", action="store_true")
     ap.add_argument("--no-warm", action="store_true")
+    ap.add_argument("--no-weighted", action="store_true")
     ap.add_argument("--tuning", default=None,
                     help="hist,part,tile,sparse,cta,subtree[,predict]: use this launch tuning for the headline "
                          "instead of autotuning it (profiling runs reuse a chosen setting)")
