@@ -1,4 +1,8 @@
-"""Writes the golden fixtures under tests/golden/ (run in a container with the reference).
+"""Writes the golden fixtures under tests/golden/ from the reference's source tree.
+
+Usage: python tests/golden/make_golden.py REFERENCE_DIR (or set ORB_REFERENCE_DIR); the
+directory is the andrinr/gpu-load-balance checkout. Without it the script stops and the
+committed fixtures stay as they are.
 
 doc_example.json: the reference thesis's worked 2-D partition example
   (andrinr/gpu-load-balance documentation/particles10.csv -> particles11.csv ->
@@ -17,11 +21,18 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DOC = "/root/reference/documentation"
+
+
+def reference_dir():
+    d = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ORB_REFERENCE_DIR")
+    if not d or not os.path.isdir(os.path.join(d, "documentation")):
+        sys.exit("make_golden.py: give the reference's checkout as an argument or in "
+                 "ORB_REFERENCE_DIR (the committed fixtures are left unchanged)")
+    return d
 
 
 def read(name):
-    with open(os.path.join(REF_DOC, name)) as f:
+    with open(os.path.join(reference_dir(), "documentation", name)) as f:
         rows = [[c.strip() for c in r] for r in csv.reader(f) if r]
     head, body = rows[0], rows[1:]
     cols = {h: [r[i] for r in body] for i, h in enumerate(head)}
