@@ -86,7 +86,6 @@ struct orb_ctx {
     DevBuf<float> cmp_keys;
     DevBuf<uint32_t> hist;
     DevBuf<uint32_t> ptile_off, ge_bits, le_bits, pt_ge, pt_le, pt_ge_pre, pt_le_pre;
-    DevBuf<uint16_t> ge_list, le_list;  // partition: positions of the keys >= / <= cut per tile
     DevBuf<unsigned long long> pt_status;
     DevBuf<int> slots;
     DevBuf<BuildCounters> counters;
@@ -183,8 +182,6 @@ orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
     ORB_CUDA(ctx->ptile_cell.ensure(ptiles));
     ORB_CUDA(ctx->ge_bits.ensure(ptiles * kPWords));
     ORB_CUDA(ctx->le_bits.ensure(ptiles * kPWords));
-    ORB_CUDA(ctx->ge_list.ensure(ptiles * kPTile));
-    ORB_CUDA(ctx->le_list.ensure(ptiles * kPTile));
     ORB_CUDA(ctx->pt_ge.ensure(ptiles));
     ORB_CUDA(ctx->pt_le.ensure(ptiles));
     ORB_CUDA(ctx->pt_ge_pre.ensure(ptiles + 1));
@@ -255,8 +252,6 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.ptile_off = ctx->ptile_off.p;
     v.ge_bits = ctx->ge_bits.p;
     v.le_bits = ctx->le_bits.p;
-    v.ge_list = ctx->ge_list.p;
-    v.le_list = ctx->le_list.p;
     v.pt_ge = ctx->pt_ge.p;
     v.pt_le = ctx->pt_le.p;
     v.pt_ge_pre = ctx->pt_ge_pre.p;
@@ -422,8 +417,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.listed, (const void *)v.cmp_keys, (const void *)v.cmp_off,
                           (const void *)v.inb, (const void *)v.htile_cell,
                           (const void *)v.ptile_cell, (const void *)v.ptile_off, (const void *)v.ge_bits,
-                          (const void *)v.le_bits, (const void *)v.ge_list, (const void *)v.le_list,
-                          (const void *)v.pt_ge, (const void *)v.pt_le,
+                          (const void *)v.le_bits, (const void *)v.pt_ge, (const void *)v.pt_le,
                           (const void *)v.pt_ge_pre, (const void *)v.pt_le_pre, (const void *)v.pt_status,
                           (const void *)v.part_s, (const void *)v.part_i, (const void *)v.part_le,
                           (const void *)v.pred, (const void *)v.counters, (const void *)v.wt,
@@ -685,7 +679,6 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->part_s.release(); ctx->part_i.release(); ctx->part_le.release(); ctx->out_counts.release();
     ctx->hist_k.release(); ctx->state.release(); ctx->iters.release(); ctx->hist.release();
     ctx->ptile_off.release(); ctx->ge_bits.release(); ctx->le_bits.release(); ctx->pt_ge.release();
-    ctx->ge_list.release(); ctx->le_list.release();
     ctx->pt_le.release(); ctx->pt_ge_pre.release(); ctx->pt_le_pre.release(); ctx->pt_status.release();
     ctx->slots.release(); ctx->counters.release(); ctx->staging.release();
     ctx->htile_cell.release(); ctx->ptile_cell.release();

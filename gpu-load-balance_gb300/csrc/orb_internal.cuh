@@ -137,8 +137,6 @@ struct Level {
     uint32_t *ptile_off;    // [C+1] first partition tile of each cell
     uint32_t *ge_bits;      // [ptiles * kPWords] bit p: key >= cut
     uint32_t *le_bits;      // [ptiles * kPWords] bit p: key <= cut
-    uint16_t *ge_list;      // [ptiles * kPTile] tile-relative positions of the keys >= cut,
-    uint16_t *le_list;      //   in order (entry j: the tile's j-th), and of the keys <= cut
     uint32_t *pt_ge;        // [ptiles] set bits per tile
     uint32_t *pt_le;
     uint32_t *pt_ge_pre;    // [ptiles+1] exclusive prefix over all tiles of the level

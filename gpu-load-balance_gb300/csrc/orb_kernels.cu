@@ -1860,11 +1860,10 @@ __device__ __forceinline__ unsigned long long pack_status(unsigned long long fla
     return flag | ((unsigned long long)g << 31) | (unsigned long long)l;
 }
 
-// P1: bitmasks of keys >= cut and keys <= cut per partition tile, their counts, and the
-// tile-relative positions of both kinds of keys in order (2 B each: the lists the swap reads
-// its pairs from). One warp per tile: the metadata chains (tile -> cell -> range, cut) of
-// the CTA's warps overlap, and each lane keeps kClassifyLoads loads in flight. The mask
-// words are staged in shared memory and stored coalesced.
+// P1: bitmasks of keys >= cut and keys <= cut per partition tile, and their counts.
+// One warp per tile: the metadata chains (tile -> cell -> range, cut) of the CTA's warps
+// overlap, and each lane keeps kClassifyLoads loads in flight. The mask words are staged in
+// shared memory and stored coalesced.
 constexpr int kClassifyLoads = 16;
 
 __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
@@ -1885,8 +1884,6 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
         const uint2 rg = v.ranges[slot];
         const uint32_t p0 = rg.x + (t - t0) * (uint32_t)kPTile;
         const uint32_t m = min((uint32_t)kPTile, rg.y - p0);
-        uint16_t *gl = v.ge_list + (size_t)t * kPTile;
-        uint16_t *ll = v.le_list + (size_t)t * kPTile;
         uint32_t cg = 0, cl = 0;
 #pragma unroll 1
         for (int r = 0; r < kPWords; r += kClassifyLoads) {
@@ -1900,17 +1897,12 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
             for (int u = 0; u < kClassifyLoads; ++u) {
                 const int w = r + u;
                 const bool valid = (uint32_t)w * 32u + lane < m;
-                const bool ge = valid && !(k[u] < cut), le = valid && !(k[u] > cut);
-                const uint32_t gb = __ballot_sync(0xffffffffu, ge);
-                const uint32_t lb = __ballot_sync(0xffffffffu, le);
+                const uint32_t gb = __ballot_sync(0xffffffffu, valid && !(k[u] < cut));
+                const uint32_t lb = __ballot_sync(0xffffffffu, valid && !(k[u] > cut));
                 if (lane == u) {
                     sw[0][w] = gb;
                     sw[1][w] = lb;
                 }
-                // the position lists the swap reads: entry (rank within the tile) = position
-                const uint32_t below = (1u << lane) - 1u;
-                if (ge) gl[cg + __popc(gb & below)] = (uint16_t)(w * 32 + lane);
-                if (le) ll[cl + __popc(lb & below)] = (uint16_t)(w * 32 + lane);
                 cg += __popc(gb);
                 cl += __popc(lb);
             }
@@ -1927,7 +1919,7 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
         if (lane == 0) {
             v.pt_ge[t] = cg;
             v.pt_le[t] = cl;
-            bytes += 4ull * m + 8ull * kPWords + 8ull + 2ull * (cg + cl);
+            bytes += 4ull * m + 8ull * kPWords + 8ull;
         }
     }
     if (lane == 0 && bytes) add_bytes(v, kKPartClassify, bytes);
@@ -2125,6 +2117,27 @@ __global__ void __launch_bounds__(kThreads) k_part_cells(Level v) {
     }
 }
 
+// Writes the cell-relative positions of the set bits of one tile's mask whose in-cell rank
+// lies in [lo, hi) to out[f(rank)], f(rank) = rank - lo (forward) or (top - rank) (reverse).
+// Block-cooperative; `sh` holds >= 96 words.
+__device__ __forceinline__ void emit_positions(const uint32_t *words, uint32_t rank_base,
+                                               uint32_t lo, uint32_t hi, uint32_t rel_base,
+                                               bool reverse, uint32_t top, uint32_t *out,
+                                               uint32_t *sh) {
+    const uint32_t tid = threadIdx.x;
+    const uint32_t w = tid < (uint32_t)kPWords ? words[tid] : 0u;
+    uint32_t ta, tb;
+    const uint2 ex = block_excl_scan2(__popc(w), 0u, sh, &ta, &tb);
+    uint32_t r = rank_base + ex.x;
+    uint32_t word = w;
+    while (word) {
+        const uint32_t b = (uint32_t)(__ffs(word) - 1);
+        word &= word - 1;
+        if (r >= lo && r < hi) out[reverse ? top - r : r - lo] = rel_base + tid * 32u + b;
+        ++r;
+    }
+}
+
 __device__ __forceinline__ void swap_particles(const Level &v, uint32_t a, uint32_t b) {
     const float xa = v.x[a], xb = v.x[b];
     const float ya = v.y[a], yb = v.y[b];
@@ -2164,102 +2177,76 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
     return lo;
 }
 
-// Largest u in [u, hi] with pre[u'] - base <= r, given pre[u] - base <= r (pre
-// non-decreasing): a few steps forward (the usual case: r lies in u's tile or the next),
-// then a binary search.
-__device__ __forceinline__ uint32_t tile_of_rank(const uint32_t *pre, uint32_t base, uint32_t u,
-                                                 uint32_t hi, uint32_t r) {
-#pragma unroll 1
-    for (int step = 0; step < 3; ++step) {
-        if (u >= hi || pre[u + 1] - base > r) return u;
-        ++u;
-    }
-    uint32_t lo = u, h = hi;
-    while (lo < h) {
-        const uint32_t mid = (lo + h + 1) >> 1;
-        if (pre[mid] - base <= r)
-            lo = mid;
-        else
-            h = mid - 1;
-    }
-    return lo;
-}
-
-// P4: the Hoare swaps. The CTA of tile t takes the pairs (L_k, R_k) whose left element L_k
-// lies in t (k < s): L_k is entry k - k0 of the tile's `>=` list (k0: the cell-rank of the
-// tile's first key >= cut); its partner R_k is the key <= cut of left-to-right rank
-// r = le_tot-1-k, entry r - pre(u) of the `<=` list of the tile u that holds that rank. A
-// lane takes one pair of each of kB consecutive runs of 32 (consecutive lanes: consecutive
-// pairs, so the list reads and the particle reads of a warp are contiguous) and issues every
-// load before any store. Positions of each side are disjoint (L_k < i <= R_k): no two
-// threads touch one particle, and no thread waits for another (no block barrier).
-// Tuning (compile time): pair runs per lane, and the CTAs per SM the register budget is
-// sized for.
+// P4: the Hoare swaps. The CTA of tile t takes the pairs (L_k, R_k) whose left element
+// L_k lies in t (k < s); their right partners are the keys <= cut of left-to-right rank
+// le_tot-1-k, found in the right tiles' masks. Positions of each side are disjoint
+// (L_k < i <= R_k), so the CTAs never touch the same particle.
+// Tuning (compile time): pairs per thread per round, and the CTAs per SM the register
+// budget is sized for (4 x 256 threads: 64 registers a thread).
 #ifndef ORB_SWAP_BATCH
-#define ORB_SWAP_BATCH 3
+#define ORB_SWAP_BATCH 4
 #endif
 #ifndef ORB_SWAP_MIN_BLOCKS
 #define ORB_SWAP_MIN_BLOCKS 4
 #endif
-// kIdx: the permutation moves too; kWt: weighted builds, whose weights move with their
-// particles (separate instances, so the plain build's loop keeps its registers)
-template <bool kIdx, bool kWt>
+template <bool kWt>  // kWt: weighted builds, whose weights move with their particles
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
+    __shared__ uint32_t posL[kPTile];
+    __shared__ uint32_t posR[kPTile];
+    __shared__ uint32_t sh[96];
     const uint32_t total = v.ptile_off[v.C];
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    constexpr int kB = ORB_SWAP_BATCH;
-    unsigned long long pairs = 0;  // pairs swapped by this CTA
+    unsigned long long bytes = 0;  // pairs swapped by this CTA
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const int c = v.ptile_cell ? (int)v.ptile_cell[t] : find_cell(v.ptile_off, v.C, t);
         const uint32_t t0 = v.ptile_off[c], t1 = v.ptile_off[c + 1];
         const uint32_t s = v.part_s[c];
         const uint32_t G0 = v.pt_ge_pre[t0], L0 = v.pt_le_pre[t0];
-        const uint32_t k0 = v.pt_ge_pre[t] - G0;
+        const uint32_t ka = v.pt_ge_pre[t] - G0;
         const uint32_t kb = min(s, v.pt_ge_pre[t + 1] - G0);
-        if (k0 >= kb) continue;  // no left element of a pair in this tile
-        const uint32_t cnt = kb - k0;
+        if (ka >= kb) continue;
+        const uint32_t cnt = kb - ka;
         const uint32_t le_tot = v.part_le[c];
         const uint32_t b = v.ranges[level_slot(v, c)].x;
-        const uint16_t *gl = v.ge_list + (size_t)t * kPTile;
-        const uint32_t abase = b + (t - t0) * (uint32_t)kPTile;
-        if (threadIdx.x == 0) pairs += cnt;
-        for (uint32_t j0 = warp * 32u * kB; j0 < cnt; j0 += nwarps * 32u * kB) {
-            // the warp's smallest partner rank this round, and the tile holding it
-            const uint32_t jl = min(cnt, j0 + 32u * kB) - 1u;
-            const uint32_t u_w = warp_last_at_most(v.pt_le_pre, L0, t0, t1 - 1, le_tot - 1u - (k0 + jl));
+        // left elements: ranks [ka, kb) of this tile's >= mask, in order
+        emit_positions(v.ge_bits + (size_t)t * kPWords, ka, ka, kb, (t - t0) * (uint32_t)kPTile,
+                       false, 0u, posL, sh);
+        // right partners: left-to-right <= ranks [le_tot-kb, le_tot-ka); rank r pairs with
+        // k = le_tot-1-r, stored at posR[k - ka] = posR[(le_tot-1-ka) - r]
+        const uint32_t ra = le_tot - kb, rb = le_tot - ka;
+        const uint32_t u0 = warp_last_at_most(v.pt_le_pre, L0, t0, t1 - 1, ra);
+        for (uint32_t u = u0; u < t1 && v.pt_le_pre[u] - L0 < rb; ++u)
+            emit_positions(v.le_bits + (size_t)u * kPWords, v.pt_le_pre[u] - L0, ra, rb,
+                           (u - t0) * (uint32_t)kPTile, true, le_tot - 1 - ka, posR, sh);
+        __syncthreads();
+        // kB pairs per thread per round: every load is issued before any store
+        constexpr int kB = ORB_SWAP_BATCH;
+        for (uint32_t j0 = 0; j0 < cnt; j0 += kB * blockDim.x) {
             uint32_t pa[kB], pb[kB];
             float xa[kB], xb[kB], ya[kB], yb[kB], za[kB], zb[kB];
             uint32_t ia[kB], ib[kB], wa[kB], wb[kB];
 #pragma unroll
             for (int q = 0; q < kB; ++q) {
-                const uint32_t j = j0 + (uint32_t)q * 32u + lane;
-                pa[q] = pb[q] = 0xffffffffu;
-                if (j < cnt) {
-                    const uint32_t r = le_tot - 1u - (k0 + j);
-                    const uint32_t u = tile_of_rank(v.pt_le_pre, L0, u_w, t1 - 1, r);
-                    pa[q] = abase + gl[j];
-                    pb[q] = b + (u - t0) * (uint32_t)kPTile +
-                            v.le_list[(size_t)u * kPTile + (r - (v.pt_le_pre[u] - L0))];
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kB; ++q) {
-                if (pa[q] == 0xffffffffu) continue;
-                xa[q] = v.x[pa[q]];
-                xb[q] = v.x[pb[q]];
-                ya[q] = v.y[pa[q]];
-                yb[q] = v.y[pb[q]];
-                za[q] = v.z[pa[q]];
-                zb[q] = v.z[pb[q]];
-                if constexpr (kIdx) {
-                    ia[q] = v.idx[pa[q]];
-                    ib[q] = v.idx[pb[q]];
-                }
-                if constexpr (kWt) {
-                    wa[q] = v.wt[pa[q]];
-                    wb[q] = v.wt[pb[q]];
+                const uint32_t j = j0 + q * blockDim.x + threadIdx.x;
+                const bool ok = j < cnt;
+                pa[q] = ok ? b + posL[j] : 0xffffffffu;
+                pb[q] = ok ? b + posR[j] : 0xffffffffu;
+                if (ok) {
+                    xa[q] = v.x[pa[q]];
+                    xb[q] = v.x[pb[q]];
+                    ya[q] = v.y[pa[q]];
+                    yb[q] = v.y[pb[q]];
+                    za[q] = v.z[pa[q]];
+                    zb[q] = v.z[pb[q]];
+                    if (v.idx) {
+                        ia[q] = v.idx[pa[q]];
+                        ib[q] = v.idx[pb[q]];
+                    }
+                    if constexpr (kWt) {
+                        wa[q] = v.wt[pa[q]];
+                        wb[q] = v.wt[pb[q]];
+                    }
                 }
             }
 #pragma unroll
@@ -2271,7 +2258,7 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                 v.y[pb[q]] = ya[q];
                 v.z[pa[q]] = zb[q];
                 v.z[pb[q]] = za[q];
-                if constexpr (kIdx) {
+                if (v.idx) {
                     v.idx[pa[q]] = ib[q];
                     v.idx[pb[q]] = ia[q];
                 }
@@ -2281,10 +2268,12 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                 }
             }
         }
+        bytes += cnt;
+        __syncthreads();
     }
     // per pair: both elements of x, y, z (and idx, weights) read and written
-    if (threadIdx.x == 0 && pairs)
-        add_bytes(v, kKPartSwap, (48ull + (kIdx ? 16ull : 0ull) + (kWt ? 16ull : 0ull)) * pairs);
+    if (threadIdx.x == 0 && bytes)
+        add_bytes(v, kKPartSwap, (48ull + (v.idx ? 16ull : 0ull) + (kWt ? 16ull : 0ull)) * bytes);
 }
 
 __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {
@@ -3183,11 +3172,9 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
             break;
         case kKPartSwap:
             if (v.wt)
-                v.idx ? k_part_swap<true, true><<<grid, kThreads, 0, st>>>(v)
-                      : k_part_swap<false, true><<<grid, kThreads, 0, st>>>(v);
+                k_part_swap<true><<<grid, kThreads, 0, st>>>(v);
             else
-                v.idx ? k_part_swap<true, false><<<grid, kThreads, 0, st>>>(v)
-                      : k_part_swap<false, false><<<grid, kThreads, 0, st>>>(v);
+                k_part_swap<false><<<grid, kThreads, 0, st>>>(v);
             break;
         case kKWStart: k_wstart<<<grid, kThreads, 0, st>>>(v); break;
         case kKWHist: k_whist<<<grid, kThreads, 0, st>>>(v); break;
