@@ -95,6 +95,7 @@ struct BuildCounters {
     uint32_t warm_resets; // ... whose hinted bracket missed the target (restarted cold)
     uint32_t pred_cells;  // cells whose first count pass used a sampled bracket
     uint32_t pred_misses; // ... whose sampled bracket did not hold the cut (binned again)
+    uint32_t sub_next;    // next root cell of the subtree kernel's work queue
     unsigned long long bytes[32];  // algorithmic bytes per Kernel kind
 };
 

@@ -2370,6 +2370,7 @@ struct SubSmem {
     uint32_t red[96];
     int queue[2][kSubQueue];
     uint32_t word, count;                            // broadcast values
+    int root;                                        // the CTA's current root cell
 };
 
 // Position of the bit of rank r (0-based) in w (r < popc(w)).
@@ -2713,6 +2714,142 @@ __device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned lo
     __syncthreads();
 }
 
+// ---- small cells (at most kWarpKeys particles) by one warp each, inside the subtree kernel:
+// the same bisection and Hoare characterisation as sub_bisect / sub_partition, with the
+// cell's keys in the warp's registers (lane l holds positions 32 j + l) and its masks one
+// word a lane, so the CTA's warps finish eight small cells at once.
+
+// Position of the set bit of rank r in the warp's mask (lane w holds word w, pre = its
+// exclusive prefix popcount, W words). Every lane returns the answer.
+__device__ __forceinline__ uint32_t warp_mask_select(uint32_t word, uint32_t pre, uint32_t W,
+                                                     uint32_t lane, uint32_t r) {
+    const uint32_t w = (uint32_t)__popc(__ballot_sync(0xffffffffu, lane < W && pre <= r)) - 1u;
+    const uint32_t ww = __shfl_sync(0xffffffffu, word, (int)w);
+    const uint32_t pw = __shfl_sync(0xffffffffu, pre, (int)w);
+    return w * 32u + select_in_word(ww, r - pw);
+}
+
+// The bisection of one small cell by the calling warp (src/orbit.cpp:146-232).
+__device__ __noinline__ void warp_bisect_cell(const Level &v, int slot, uint32_t lane, unsigned long long &bytes) {
+    orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x;
+    const float ratio = 0.5f;  // subtrees: powers of two only (leaf_ratio of an even count)
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    float k[kWarpKeysPerLane];
+#pragma unroll
+    for (int j = 0; j < kWarpKeysPerLane; ++j) {
+        const uint32_t i = (uint32_t)(j * 32) + lane;
+        k[j] = i < n ? keys[rg.x + i] : __int_as_float(0x7fc00000);  // coherent: moved here
+    }
+    float L = cell.cutMarginLeft, R = cell.cutMarginRight;
+    uint32_t it = 0;
+    int st = kActive;
+    while (st == kActive) {
+        if (it >= (uint32_t)kMaxIterations) {
+            st = kCapped;
+            break;
+        }
+        const float cut = mid_cut(L, R);
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kWarpKeysPerLane; ++j) cnt += k[j] < cut;
+        cnt = warp_sum(cnt);
+        ++it;
+        const int dir = convergence(cnt, n, ratio);
+        if (dir == 0)
+            st = kFound;
+        else if (dir > 0)
+            R = cut;
+        else
+            L = cut;
+    }
+    if (lane == 0) {
+        cell.cutMarginLeft = L;
+        cell.cutMarginRight = R;
+        cell.foundCut = st == kFound ? 1 : 0;
+        atomicMax(&v.counters->max_iters, it);
+        if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
+        bytes += 4ull * n;
+    }
+    __syncwarp();
+}
+
+// The Hoare partition (src/services/partition.cpp:30-52) of one small cell by the calling
+// warp: masks of keys >= cut and <= cut (word w: positions 32 w .. 32 w + 31), the swap count
+// s from the word where the two counts cross, the pairs (L_k, R_k) k < s swapped lane by
+// lane, then i = min(L_{s+1}, R_s) and the final swap and split by lane 0 (finish_cell).
+__device__ __noinline__ void warp_partition_cell(const Level &v, int slot, uint32_t lane, unsigned long long &bytes) {
+    const orb_cell_t &cell = v.heap[slot];
+    const uint2 rg = v.ranges[slot];
+    const uint32_t n = rg.y - rg.x, b = rg.x;
+    const float *keys = axis_keys(v, eff_axis(cell.cutAxis));
+    const float cut = cell_cut(cell);
+    const uint32_t W = (n + 31) / 32;
+    uint32_t gw = 0, lw = 0;  // this lane's words (w = lane)
+    for (uint32_t w = 0; w < W; ++w) {
+        const uint32_t i = w * 32u + lane;
+        const float k = i < n ? keys[b + i] : 0.0f;  // coherent: moved here
+        const uint32_t gb = __ballot_sync(0xffffffffu, i < n && !(k < cut));
+        const uint32_t lb = __ballot_sync(0xffffffffu, i < n && !(k > cut));
+        if (lane == w) {
+            gw = gb;
+            lw = lb;
+        }
+    }
+    uint32_t ge_tot, le_tot;
+    const uint32_t pge = warp_excl_scan((uint32_t)__popc(gw), &ge_tot);
+    const uint32_t ple = warp_excl_scan((uint32_t)__popc(lw), &le_tot);
+    // s = max over x of min(#>= in [0,x), #<= in [x,n)): it lies in the first word at whose end
+    // f >= g (f rises, g falls)
+    uint32_t s = 0;
+    if (W > 0) {
+        const bool cross = lane < W && pge + (uint32_t)__popc(gw) >= le_tot - ple - (uint32_t)__popc(lw);
+        const uint32_t cb = __ballot_sync(0xffffffffu, cross);
+        const int w = cb ? __ffs(cb) - 1 : (int)W - 1;
+        uint32_t f = __shfl_sync(0xffffffffu, pge, w), g = le_tot - __shfl_sync(0xffffffffu, ple, w);
+        uint32_t a = __shfl_sync(0xffffffffu, gw, w), c = __shfl_sync(0xffffffffu, lw, w);
+        s = min(f, g);
+        for (int q = 0; q < 32; ++q) {
+            f += a & 1u;
+            g -= c & 1u;
+            a >>= 1;
+            c >>= 1;
+            s = max(s, min(f, g));
+        }
+    }
+    uint32_t i = n;  // split index, n when every key is below the cut
+    if (ge_tot > s) i = min(i, warp_mask_select(gw, pge, W, lane, s));
+    if (s >= 1) i = min(i, warp_mask_select(lw, ple, W, lane, le_tot - s));
+    for (uint32_t k0 = 0; k0 < s; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        const uint32_t kk = k < s ? k : s - 1;  // every lane runs the selects (shuffles)
+        const uint32_t pa = b + warp_mask_select(gw, pge, W, lane, kk);
+        const uint32_t pb = b + warp_mask_select(lw, ple, W, lane, le_tot - 1 - kk);
+        if (k < s) {
+            const float xa = v.x[pa], xb = v.x[pb], ya = v.y[pa], yb = v.y[pb];
+            const float za = v.z[pa], zb = v.z[pb];
+            v.x[pa] = xb;
+            v.x[pb] = xa;
+            v.y[pa] = yb;
+            v.y[pb] = ya;
+            v.z[pa] = zb;
+            v.z[pb] = za;
+            if (v.idx) {
+                const uint32_t ia = v.idx[pa], ib = v.idx[pb];
+                v.idx[pa] = ib;
+                v.idx[pb] = ia;
+            }
+        }
+    }
+    __syncwarp();  // the swaps are visible to lane 0's final swap
+    if (lane == 0) {
+        bytes += (v.idx ? 64ull : 48ull) * s + 4ull * n;
+        finish_cell(v, slot, i, true);
+    }
+    __syncwarp();
+}
+
 // Levels below a cell in a full build: log2 of its leaf count (d is a power of two).
 __device__ __forceinline__ int levels_below(const orb_cell_t &c) {
     return c.nLeafCells > 1 ? 31 - __clz((uint32_t)c.nLeafCells) : 0;
@@ -2764,28 +2901,45 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
     unsigned long long bytes = 0;
-    for (int c = blockIdx.x; c < v.C; c += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        // root cells from a queue: CTAs that finish small (or clustered) cells take more
+        if (threadIdx.x == 0) sm.root = (int)atomicAdd(&v.counters->sub_next, 1u);
+        __syncthreads();
+        const int c = sm.root;
+        if (c >= v.C) break;
         int cur = 0, nq = 1;
         const int root = level_slot(v, c);
         const int levels = levels_below(v.heap[root]);
         if (threadIdx.x == 0) sm.queue[0][0] = root;
         __syncthreads();
         for (int l = 0; l < levels; ++l) {
-            int nn = 0;
+            // children of queue entry q at 2q, 2q+1 of the next level's queue
+            if ((int)threadIdx.x < nq && 2 * (int)threadIdx.x + 2 <= kSubQueue) {
+                const int slot = sm.queue[cur][threadIdx.x];
+                const int id = v.heap[slot].id;
+                sm.queue[cur ^ 1][2 * threadIdx.x] = slot + id + 1;
+                sm.queue[cur ^ 1][2 * threadIdx.x + 1] = slot + id + 2;
+            }
+            // cells of more than kWarpKeys particles by the whole CTA, one after the other
             for (int q = 0; q < nq; ++q) {
                 const int slot = sm.queue[cur][q];
+                const uint2 rg = v.ranges[slot];
+                if (rg.y - rg.x <= (uint32_t)kWarpKeys) continue;  // CTA-uniform
                 sub_bisect(v, slot, sm, bytes);
                 sub_partition(v, slot, sm, bytes);
-                if (threadIdx.x == 0 && nn + 2 <= kSubQueue) {
-                    const int id = v.heap[slot].id;
-                    sm.queue[cur ^ 1][nn] = slot + id + 1;
-                    sm.queue[cur ^ 1][nn + 1] = slot + id + 2;
-                }
-                nn += 2;
+            }
+            // the small ones by one warp each, the CTA's warps side by side
+            for (int q = (int)warp; q < nq; q += (int)nwarps) {
+                const int slot = sm.queue[cur][q];
+                const uint2 rg = v.ranges[slot];
+                if (rg.y - rg.x > (uint32_t)kWarpKeys) continue;  // warp-uniform
+                warp_bisect_cell(v, slot, lane, bytes);
+                warp_partition_cell(v, slot, lane, bytes);
             }
             __syncthreads();
             cur ^= 1;
-            nq = nn;
+            nq = 2 * nq;
         }
         if (v.hx) {  // the cell's particles are final: to the caller's host arrays
             const uint2 rg = v.ranges[root];
@@ -2795,7 +2949,8 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
             if (v.hperm && v.idx) copy_out(v.idx, v.hperm, rg.x, rg.y);
         }
     }
-    if (threadIdx.x == 0 && bytes) add_bytes(v, kKSubtree, bytes);
+    // lane 0 of every warp counted the small cells its warp finished (thread 0 the rest too)
+    if (lane == 0 && bytes) add_bytes(v, kKSubtree, bytes);
 }
 
 // ------------------------------------------------------------------------------------
