@@ -516,7 +516,10 @@ orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, u
             if (v.C == 0) break;
             v.skip = ctx->sub_flag.p;
             run_kernel(ctx, kKSubtreeCheck, v, 1, (int)(lv.size() - li));
-            run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm));
+            // the warp path for small cells when the deepest split cells can be that small
+            // (about max_n >> (levels - 1) particles, twice kWarpKeys allowing for uneven cells)
+            const bool small = (max_n >> (lv.size() - 1)) <= 2ull * kWarpKeys;
+            run_kernel(ctx, kKSubtree, v, std::min(v.C, ctx->num_sms * kSubtreeBlocksPerSm), small ? 1 : 0);
             break;
         }
         if (v.C == 0) continue;

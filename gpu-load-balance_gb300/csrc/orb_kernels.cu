@@ -2720,13 +2720,26 @@ __device__ void sub_partition(const Level &v, int slot, SubSmem &sm, unsigned lo
 // word a lane, so the CTA's warps finish eight small cells at once.
 
 // Position of the set bit of rank r in the warp's mask (lane w holds word w, pre = its
-// exclusive prefix popcount, W words). Every lane returns the answer.
+// exclusive prefix popcount, W <= 32 words); r may differ from lane to lane: each lane
+// searches the lanes' prefixes for the last word with pre <= r (5 shuffle steps, every lane
+// taking part in every shuffle).
 __device__ __forceinline__ uint32_t warp_mask_select(uint32_t word, uint32_t pre, uint32_t W,
-                                                     uint32_t lane, uint32_t r) {
-    const uint32_t w = (uint32_t)__popc(__ballot_sync(0xffffffffu, lane < W && pre <= r)) - 1u;
-    const uint32_t ww = __shfl_sync(0xffffffffu, word, (int)w);
-    const uint32_t pw = __shfl_sync(0xffffffffu, pre, (int)w);
-    return w * 32u + select_in_word(ww, r - pw);
+                                                     uint32_t r) {
+    int lo = 0, hi = (int)W - 1;
+#pragma unroll
+    for (int step = 0; step < 5; ++step) {
+        const int mid = (lo + hi + 1) >> 1;
+        const uint32_t pm = __shfl_sync(0xffffffffu, pre, mid);
+        if (lo < hi) {
+            if (pm <= r)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+    }
+    const uint32_t ww = __shfl_sync(0xffffffffu, word, lo);
+    const uint32_t pw = __shfl_sync(0xffffffffu, pre, lo);
+    return (uint32_t)lo * 32u + select_in_word(ww, r - pw);
 }
 
 // The bisection of one small cell by the calling warp (src/orbit.cpp:146-232).
@@ -2819,13 +2832,13 @@ __device__ __noinline__ void warp_partition_cell(const Level &v, int slot, uint3
         }
     }
     uint32_t i = n;  // split index, n when every key is below the cut
-    if (ge_tot > s) i = min(i, warp_mask_select(gw, pge, W, lane, s));
-    if (s >= 1) i = min(i, warp_mask_select(lw, ple, W, lane, le_tot - s));
+    if (ge_tot > s) i = min(i, warp_mask_select(gw, pge, W, s));
+    if (s >= 1) i = min(i, warp_mask_select(lw, ple, W, le_tot - s));
     for (uint32_t k0 = 0; k0 < s; k0 += 32) {
         const uint32_t k = k0 + lane;
         const uint32_t kk = k < s ? k : s - 1;  // every lane runs the selects (shuffles)
-        const uint32_t pa = b + warp_mask_select(gw, pge, W, lane, kk);
-        const uint32_t pb = b + warp_mask_select(lw, ple, W, lane, le_tot - 1 - kk);
+        const uint32_t pa = b + warp_mask_select(gw, pge, W, kk);
+        const uint32_t pb = b + warp_mask_select(lw, ple, W, le_tot - 1 - kk);
         if (k < s) {
             const float xa = v.x[pa], xb = v.x[pb], ya = v.y[pa], yb = v.y[pb];
             const float za = v.z[pa], zb = v.z[pb];
@@ -2897,16 +2910,26 @@ __device__ void copy_out(const T *src, T *dst, uint32_t b, uint32_t e) {
 
 // One CTA per cell of the level: every level below it (its leaf count's log2), breadth
 // first; with host outputs (v.hx), the finished cell's particles are then written there.
+// kWarpSmall: cells of at most kWarpKeys particles go to one warp each (the CTA's warps side
+// by side); without it every cell is the whole CTA's (the instance for trees whose cells
+// never get that small keeps its registers for the CTA path). Same results either way.
+template <bool kWarpSmall>
 __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
     unsigned long long bytes = 0;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (;;) {
-        // root cells from a queue: CTAs that finish small (or clustered) cells take more
-        if (threadIdx.x == 0) sm.root = (int)atomicAdd(&v.counters->sub_next, 1u);
-        __syncthreads();
-        const int c = sm.root;
+    for (int k = 0;; ++k) {
+        // root cells: from a queue where cells can be small or uneven (CTAs that finish small
+        // cells take more), else one in gridDim.x
+        int c;
+        if constexpr (kWarpSmall) {
+            if (threadIdx.x == 0) sm.root = (int)atomicAdd(&v.counters->sub_next, 1u);
+            __syncthreads();
+            c = sm.root;
+        } else {
+            c = (int)blockIdx.x + k * (int)gridDim.x;
+        }
         if (c >= v.C) break;
         int cur = 0, nq = 1;
         const int root = level_slot(v, c);
@@ -2925,12 +2948,12 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
             for (int q = 0; q < nq; ++q) {
                 const int slot = sm.queue[cur][q];
                 const uint2 rg = v.ranges[slot];
-                if (rg.y - rg.x <= (uint32_t)kWarpKeys) continue;  // CTA-uniform
+                if (kWarpSmall && rg.y - rg.x <= (uint32_t)kWarpKeys) continue;  // CTA-uniform
                 sub_bisect(v, slot, sm, bytes);
                 sub_partition(v, slot, sm, bytes);
             }
             // the small ones by one warp each, the CTA's warps side by side
-            for (int q = (int)warp; q < nq; q += (int)nwarps) {
+            for (int q = (int)warp; kWarpSmall && q < nq; q += (int)nwarps) {
                 const int slot = sm.queue[cur][q];
                 const uint2 rg = v.ranges[slot];
                 if (rg.y - rg.x > (uint32_t)kWarpKeys) continue;  // warp-uniform
@@ -3312,7 +3335,12 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
         case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
         case kKSubtreeCheck: k_subtree_check<<<1, 1024, 0, st>>>(v, arg); break;
-        case kKSubtree: k_subtree<<<grid, kSubThreads, 0, st>>>(v); break;
+        case kKSubtree:  // arg: 1 when cells of at most kWarpKeys particles can occur
+            if (arg)
+                k_subtree<true><<<grid, kSubThreads, 0, st>>>(v);
+            else
+                k_subtree<false><<<grid, kSubThreads, 0, st>>>(v);
+            break;
         case kKBisectCta:
             k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
             break;
