@@ -2937,8 +2937,9 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
         if (threadIdx.x == 0) sm.queue[0][0] = root;
         __syncthreads();
         for (int l = 0; l < levels; ++l) {
-            // children of queue entry q at 2q, 2q+1 of the next level's queue
-            if ((int)threadIdx.x < nq && 2 * (int)threadIdx.x + 2 <= kSubQueue) {
+            // children of queue entry q at 2q, 2q+1 of the next level's queue (the warp path:
+            // here, before the cells are processed in any order; else after each cell below)
+            if (kWarpSmall && (int)threadIdx.x < nq && 2 * (int)threadIdx.x + 2 <= kSubQueue) {
                 const int slot = sm.queue[cur][threadIdx.x];
                 const int id = v.heap[slot].id;
                 sm.queue[cur ^ 1][2 * threadIdx.x] = slot + id + 1;
@@ -2951,6 +2952,11 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
                 if (kWarpSmall && rg.y - rg.x <= (uint32_t)kWarpKeys) continue;  // CTA-uniform
                 sub_bisect(v, slot, sm, bytes);
                 sub_partition(v, slot, sm, bytes);
+                if (!kWarpSmall && threadIdx.x == 0 && 2 * q + 2 <= kSubQueue) {
+                    const int id = v.heap[slot].id;
+                    sm.queue[cur ^ 1][2 * q] = slot + id + 1;
+                    sm.queue[cur ^ 1][2 * q + 1] = slot + id + 2;
+                }
             }
             // the small ones by one warp each, the CTA's warps side by side
             for (int q = (int)warp; kWarpSmall && q < nq; q += (int)nwarps) {
