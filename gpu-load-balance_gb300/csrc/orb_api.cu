@@ -124,6 +124,8 @@ struct orb_ctx {
     // CUDA graphs of recent builds' device work (most recent first), replayed when the
     // configuration matches
     bool use_graphs = true;
+    // level kernels launched with programmatic dependent launch (ORB_NO_PDL=1: plain launches)
+    bool use_pdl = true;
     struct Graph {
         std::vector<uint64_t> key;
         cudaGraph_t graph = nullptr;
@@ -264,6 +266,7 @@ Level make_level(orb_ctx *ctx, float *x, float *y, float *z) {
     v.out_counts = ctx->out_counts.p;
     v.sparse_per_tile = ctx->tune.sparse_keys_per_tile;
     v.spin_limit = ctx->spin_limit;
+    v.pdl = ctx->use_pdl ? 1 : 0;
     v.counters = ctx->counters.p;
     return v;
 }
@@ -426,6 +429,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
     key.push_back((uint64_t)ctx->pt_status.cap);
     key.push_back(ctx->prof_mask);
     key.push_back(((uint64_t)ctx->spin_limit << 8) | ctx->scan_ticket_start);
+    key.push_back(ctx->use_pdl ? 1u : 0u);
     for (uint32_t t : {ctx->tune.hist_blocks_per_sm, ctx->tune.part_blocks_per_sm, ctx->tune.tile_blocks_per_sm,
                        ctx->tune.sparse_keys_per_tile, ctx->tune.cta_min_cells, ctx->tune.subtree_levels,
                        ctx->tune.predict_sigmas})
@@ -647,6 +651,8 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             ctx->tune.cta_min_cells = env ? (uint32_t)std::max(0, std::atoi(env)) : 0u;
             const char *ng = std::getenv("ORB_NO_GRAPHS");
             ctx->use_graphs = !(ng && ng[0] && ng[0] != '0');
+            const char *np = std::getenv("ORB_NO_PDL");
+            ctx->use_pdl = !(np && np[0] && np[0] != '0');
         }
         if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess ||
             (e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_sub_flag), sizeof(uint32_t))) != cudaSuccess) {

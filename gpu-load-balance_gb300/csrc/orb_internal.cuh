@@ -150,6 +150,7 @@ struct Level {
     uint32_t *out_counts;   // service calls: per-cell result
     uint32_t sparse_per_tile;  // count pass: sparse once the bracket holds <= this x tiles keys
     uint32_t spin_limit;    // polls of one look-back wait before it gives up (error flag)
+    int pdl;                // level kernels launched with programmatic dependent launch
     // warm builds (null otherwise): per heap slot the previous tree's cut and w x its extent
     // (x NaN: no hint) and that tree's cut axis
     const float2 *hint;     // (cut, w x extent) from the previous tree

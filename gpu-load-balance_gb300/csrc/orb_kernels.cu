@@ -38,6 +38,16 @@ __device__ __forceinline__ void add_bytes(const Level &v, Kernel k, unsigned lon
     atomicAdd(&v.counters->bytes[k], b);
 }
 
+// Programmatic dependent launch (level kernels are launched with it): wait until the
+// previous kernel of the stream has finished and its writes are visible, then let the next
+// kernel's CTAs be scheduled as this kernel's CTAs retire (its launch and ramp-up overlap
+// this kernel's tail). Every level kernel calls this before it reads anything a previous
+// kernel wrote; without a programmatic dependency both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
 // ------------------------------------------------------------------------------------
 // Block helpers
 // ------------------------------------------------------------------------------------
@@ -299,6 +309,7 @@ __device__ __forceinline__ void warm_reset(orb_cell_t &cell, float &L, float &R,
 // Plan: per-cell tile and histogram offsets (single CTA, any C).
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_plan(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t sh[96];
     const int C = v.C, tid = threadIdx.x, nt = blockDim.x;
@@ -341,6 +352,7 @@ __global__ void __launch_bounds__(1024) k_plan(Level v) {
 // the hinted bracket (clipped to its extent) when that narrows it. Its first count pass is
 // then sparse: most keys lie outside. One thread per cell.
 __global__ void k_warm_start(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     uint32_t nwarm = 0;
@@ -944,6 +956,7 @@ __device__ __forceinline__ uint32_t sample_count(uint32_t n) {
 // between passes) by the scaled guess or the descent; samples below L are counted in
 // pred[c], which k_sample_pick then replaces by the prediction.
 __global__ void __launch_bounds__(kSampleThreads) k_sample_bin(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const uint32_t ti = threadIdx.x;
     for (int c = blockIdx.y; c < v.C; c += gridDim.y) {
@@ -993,6 +1006,7 @@ __global__ void __launch_bounds__(kSampleThreads) k_sample_bin(Level v) {
 constexpr int kPickThreads = 256;
 static_assert((1 << kMaxBinsLog2) == 8 * kPickThreads, "8 bins a thread");
 __global__ void __launch_bounds__(kPickThreads) k_sample_pick(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_red[72];
     const uint32_t ti = threadIdx.x;
@@ -1082,6 +1096,7 @@ constexpr uint32_t kHFirstSampled = kHDense | kHPred | kHCompact;
 constexpr uint32_t kHRest = kHDense | kHLocal | kHCompact | kHListed | kHSparse;
 template <uint32_t Allowed>
 __global__ void __launch_bounds__(kThreads, kHistBlocksPerSm) k_hist(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     constexpr bool kAny = Allowed != kHDense;
     __shared__ uint32_t s_hist[(1 << kMaxBinsLog2) + 32];  // + the dense loop's spare bins
@@ -1323,6 +1338,7 @@ constexpr int kListPerLane = 8;     // bracket keys a lane can hold
 constexpr uint32_t kListKeys = 64;  // bracket size that switches to the register list
 
 __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_bins[kThreads / 32][kTileBins];
     __shared__ float s_edges[kThreads / 32][kTileBins + 1];
@@ -1483,6 +1499,7 @@ __global__ void __launch_bounds__(kThreads, kTileBlocksPerSm) k_bisect_tile(Leve
 // Resolve: replay up to K bisection iterations per cell on its histogram (warp per cell).
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_resolve(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -1658,6 +1675,7 @@ constexpr size_t kCtaSmemBytes = kListCap * sizeof(float) +
                                  ((1u << kMaxBinsLog2) + 1) * sizeof(float);
 
 __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     extern __shared__ __align__(16) unsigned char cta_smem[];
     float *list = reinterpret_cast<float *>(cta_smem);
@@ -1813,6 +1831,7 @@ __global__ void __launch_bounds__(kCtaThreads) k_bisect_cta(Level v) {
 // Tile -> cell maps of the level (one binary search per tile, once per level).
 // ... and the per-cell state of the level, in parallel (the plan only computes the offsets).
 __global__ void k_tile_map(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     const uint32_t ht = v.tile_off[v.C], pt = v.ptile_off[v.C], C = (uint32_t)v.C;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < max(max(ht, pt), C);
@@ -1867,6 +1886,7 @@ __device__ __forceinline__ unsigned long long pack_status(unsigned long long fla
 constexpr int kClassifyLoads = 16;
 
 __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t s_words[kThreads / 32][2][kPWords];
     const uint32_t total = v.ptile_off[v.C];
@@ -1933,6 +1953,7 @@ __global__ void __launch_bounds__(kThreads) k_part_classify(Level v) {
 constexpr int kScanBlock = 1024;
 
 __global__ void __launch_bounds__(kScanBlock) k_tile_scan(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     __shared__ uint32_t sh[96];
     __shared__ uint32_t s_b;
@@ -2053,6 +2074,7 @@ __device__ __forceinline__ bool scan_failed(const Level &v) {
 //   s = max_x min(f(x), g(x)), f(x) = #{>= cut in [0,x)}, g(x) = #{<= cut in [x,n)}
 //   i = min(L_{s+1}, R_s); i == n marks the clamped case (every key below the cut).
 __global__ void __launch_bounds__(kThreads) k_part_cells(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -2191,6 +2213,7 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #endif
 template <bool kWt>  // kWt: weighted builds, whose weights move with their particles
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     __shared__ uint32_t posL[kPTile];
@@ -2337,6 +2360,7 @@ __device__ void finish_cell(const Level &v, int slot, uint32_t i, bool do_split)
 
 // P5: finish_cell for every cell of the level.
 __global__ void __launch_bounds__(kThreads) k_part_finish(Level v, int do_split) {
+    pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2873,6 +2897,7 @@ __device__ __forceinline__ int levels_below(const orb_cell_t &c) {
 constexpr int kSubLevels = kSubMaxLevels;
 static_assert((2 << (kSubLevels - 1)) <= kSubQueue, "the last level's children fit the queue");
 __global__ void __launch_bounds__(1024) k_subtree_check(Level v, int max_levels) {
+    pdl_enter();
     __shared__ uint32_t sh[96];
     uint32_t mx = 0, ml = 0;
     for (int c = threadIdx.x; c < v.C; c += blockDim.x) {
@@ -2915,6 +2940,7 @@ __device__ void copy_out(const T *src, T *dst, uint32_t b, uint32_t e) {
 // never get that small keeps its registers for the CTA path). Same results either way.
 template <bool kWarpSmall>
 __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
+    pdl_enter();
     __shared__ SubSmem sm;
     if (*(volatile const uint32_t *)v.skip == 0u) return;  // the level kernels run instead
     unsigned long long bytes = 0;
@@ -2992,6 +3018,7 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
 // test. Integer sums: the same results in any order.
 // ------------------------------------------------------------------------------------
 __global__ void k_wstart(Level v) {
+    pdl_enter();
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < (uint32_t)v.C;
          c += gridDim.x * blockDim.x) {
         v.state[c] = kActive;
@@ -3018,6 +3045,7 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x
 }
 
 __global__ void __launch_bounds__(kThreads) k_whist(Level v) {
+    pdl_enter();
     __shared__ unsigned long long s_bins[kWBins];
     __shared__ unsigned long long s_red[kThreads / 32];
     const uint32_t total = v.tile_off[v.C];
@@ -3060,6 +3088,7 @@ __global__ void __launch_bounds__(kThreads) k_whist(Level v) {
 // pass's weight bins, with the weighted test; the bins and the weight below are cleared for
 // the next pass.
 __global__ void __launch_bounds__(kThreads) k_wresolve(Level v) {
+    pdl_enter();
     __shared__ unsigned long long s_pre[kThreads / 32][kWBins];
     const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -3136,6 +3165,7 @@ __global__ void __launch_bounds__(kThreads) k_wresolve(Level v) {
 // Service count-left: one plain pass at getCut() per cell, found cells skipped.
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_count_left(Level v) {
+    pdl_enter();
     __shared__ uint32_t s_red[32];
     const uint32_t total = v.tile_off[v.C];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
@@ -3327,57 +3357,81 @@ void launch_init(const Level &v, uint64_t n, const float lower[3], const float u
                                                         heap_cells);
 }
 
+// A level kernel on the stream, with the programmatic-dependent-launch attribute when the
+// context uses it (the kernels wait for their predecessor in pdl_enter()).
+template <class... P, class... A>
+void launch_kernel(bool pdl, void (*kern)(P...), dim3 grid, dim3 block, size_t smem,
+                   cudaStream_t st, A... args) {
+    if (!pdl) {
+        kern<<<grid, block, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream_t st) {
+    const bool p = v.pdl != 0;
+    const dim3 T(kThreads);
+    const unsigned per_cell_warps = (unsigned)grid_for((uint64_t)v.C * 32, kThreads, 1 << 30);
     switch (k) {
-        case kKPlan: k_plan<<<1, 1024, 0, st>>>(v); break;
+        case kKPlan: launch_kernel(p, k_plan, dim3(1), dim3(1024), 0, st, v); break;
         case kKHist:  // arg: 1 first pass, all cells dense; 2 first pass of a sampled level
             if (arg == 1)
-                k_hist<kHFirstDense><<<grid, kThreads, 0, st>>>(v);
+                launch_kernel(p, k_hist<kHFirstDense>, dim3(grid), T, 0, st, v);
             else if (arg == 2)
-                k_hist<kHFirstSampled><<<grid, kThreads, 0, st>>>(v);
+                launch_kernel(p, k_hist<kHFirstSampled>, dim3(grid), T, 0, st, v);
             else
-                k_hist<kHRest><<<grid, kThreads, 0, st>>>(v);
+                launch_kernel(p, k_hist<kHRest>, dim3(grid), T, 0, st, v);
             break;
-        case kKBisectTile: k_bisect_tile<<<grid, kThreads, 0, st>>>(v); break;
-        case kKWarmStart: k_warm_start<<<grid_for((uint64_t)v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v); break;
-        case kKSubtreeCheck: k_subtree_check<<<1, 1024, 0, st>>>(v, arg); break;
+        case kKBisectTile: launch_kernel(p, k_bisect_tile, dim3(grid), T, 0, st, v); break;
+        case kKWarmStart:
+            launch_kernel(p, k_warm_start, dim3(grid_for((uint64_t)v.C, kThreads, 1 << 30)), T, 0, st, v);
+            break;
+        case kKSubtreeCheck: launch_kernel(p, k_subtree_check, dim3(1), dim3(1024), 0, st, v, arg); break;
         case kKSubtree:  // arg: 1 when cells of at most kWarpKeys particles can occur
             if (arg)
-                k_subtree<true><<<grid, kSubThreads, 0, st>>>(v);
+                launch_kernel(p, k_subtree<true>, dim3(grid), dim3(kSubThreads), 0, st, v);
             else
-                k_subtree<false><<<grid, kSubThreads, 0, st>>>(v);
+                launch_kernel(p, k_subtree<false>, dim3(grid), dim3(kSubThreads), 0, st, v);
             break;
         case kKBisectCta:
-            k_bisect_cta<<<grid, kCtaThreads, kCtaSmemBytes, st>>>(v);
+            launch_kernel(p, k_bisect_cta, dim3(grid), dim3(kCtaThreads), kCtaSmemBytes, st, v);
             break;
-        case kKTileMap: k_tile_map<<<grid, kThreads, 0, st>>>(v); break;
-        case kKResolve:
-            k_resolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-            break;
-        case kKPartClassify: k_part_classify<<<grid, kThreads, 0, st>>>(v); break;
-        case kKPartScan: k_tile_scan<<<arg, kScanBlock, 0, st>>>(v); break;
-        case kKPartCells:
-            k_part_cells<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-            break;
+        case kKTileMap: launch_kernel(p, k_tile_map, dim3(grid), T, 0, st, v); break;
+        case kKResolve: launch_kernel(p, k_resolve, dim3(per_cell_warps), T, 0, st, v); break;
+        case kKPartClassify: launch_kernel(p, k_part_classify, dim3(grid), T, 0, st, v); break;
+        case kKPartScan: launch_kernel(p, k_tile_scan, dim3(arg), dim3(kScanBlock), 0, st, v); break;
+        case kKPartCells: launch_kernel(p, k_part_cells, dim3(per_cell_warps), T, 0, st, v); break;
         case kKPartSwap:
             if (v.wt)
-                k_part_swap<true><<<grid, kThreads, 0, st>>>(v);
+                launch_kernel(p, k_part_swap<true>, dim3(grid), T, 0, st, v);
             else
-                k_part_swap<false><<<grid, kThreads, 0, st>>>(v);
+                launch_kernel(p, k_part_swap<false>, dim3(grid), T, 0, st, v);
             break;
-        case kKWStart: k_wstart<<<grid, kThreads, 0, st>>>(v); break;
-        case kKWHist: k_whist<<<grid, kThreads, 0, st>>>(v); break;
-        case kKWResolve:
-            k_wresolve<<<grid_for((uint64_t)v.C * 32, kThreads, 1 << 30), kThreads, 0, st>>>(v);
-            break;
+        case kKWStart: launch_kernel(p, k_wstart, dim3(grid), T, 0, st, v); break;
+        case kKWHist: launch_kernel(p, k_whist, dim3(grid), T, 0, st, v); break;
+        case kKWResolve: launch_kernel(p, k_wresolve, dim3(per_cell_warps), T, 0, st, v); break;
         case kKPartFinish:
-            k_part_finish<<<grid_for(v.C, kThreads, 1 << 30), kThreads, 0, st>>>(v, arg);
+            launch_kernel(p, k_part_finish, dim3(grid_for(v.C, kThreads, 1 << 30)), T, 0, st, v, arg);
             break;
-        case kKCountLeft: k_count_left<<<grid, kThreads, 0, st>>>(v); break;
+        case kKCountLeft: launch_kernel(p, k_count_left, dim3(grid), T, 0, st, v); break;
         case kKSample:
-            k_sample_bin<<<dim3(kSampleMax / kSamplePerCta, (unsigned)min(v.C, 65535)), kSampleThreads, 0, st>>>(v);
+            launch_kernel(p, k_sample_bin, dim3(kSampleMax / kSamplePerCta, (unsigned)min(v.C, 65535)),
+                          dim3(kSampleThreads), 0, st, v);
             break;
-        case kKSamplePick: k_sample_pick<<<min(v.C, 65535), kPickThreads, 0, st>>>(v); break;
+        case kKSamplePick:
+            launch_kernel(p, k_sample_pick, dim3((unsigned)min(v.C, 65535)), dim3(kPickThreads), 0, st, v);
+            break;
         default: break;
     }
 }
