@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <algorithm>
 #include <cstdlib>
@@ -66,6 +67,11 @@ struct orb_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t yz_ready = nullptr;
     bool yz_pending = false;
+    // staged builds from host memory (stage_coords): y arrives in yraw while level 1 (cut
+    // along x) runs, z in zraw while level 2 runs; y_ready marks y's copy, yz_ready z's
+    cudaEvent_t y_ready = nullptr;
+    bool use_stage = true;  // ORB_NO_STAGE=1 turns staged builds off
+    DevBuf<float> yraw, zraw;
     std::string err;
 
     DevBuf<float> x, y, z;
@@ -303,6 +309,23 @@ void run_kernel(orb_ctx *ctx, Kernel k, const Level &v, int grid, int arg = 0) {
     }
 }
 
+// dst[p] = src[idx[p]] on the build stream (staged builds), timed like a level kernel.
+void run_stage_gather(orb_ctx *ctx, float *dst, const float *src, uint64_t n) {
+    ctx->launches[kKStageGather] += 1;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (ctx->prof_mask & (1u << kKStageGather)) {
+        a = take_event(ctx);
+        b = take_event(ctx);
+    }
+    const unsigned rf = ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (a && b) cudaEventRecordWithFlags(a, ctx->stream, rf);
+    launch_stage_gather(dst, src, ctx->idx.p, n, ctx->counters.p, ctx->num_sms, ctx->stream);
+    if (a && b) {
+        cudaEventRecordWithFlags(b, ctx->stream, rf);
+        ctx->recs.push_back({(int)kKStageGather, a, b});
+    }
+}
+
 // Folds finished event pairs into the per-kernel totals (stream must be idle).
 void collect_profile(orb_ctx *ctx) {
     for (auto &r : ctx->recs) {
@@ -509,9 +532,12 @@ int subtree_from(const orb_ctx *ctx, const std::vector<LevelDesc> &lv, uint64_t 
 // rest = false: the levels above sub_from, then (sub_from >= 0) the subtree check and the
 // subtree kernel for the levels from sub_from down; rest = true: the levels from sub_from
 // down one by one, for builds whose subtree path the device refused.
+// [from, to): only those levels (staged builds run the levels in three pieces).
 orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes,
-                      int sub_from, uint64_t max_n, bool rest = false) {
-    for (size_t li = rest ? (size_t)sub_from : 0; li < lv.size(); ++li) {
+                      int sub_from, uint64_t max_n, bool rest = false, size_t from = 0,
+                      size_t to = SIZE_MAX) {
+    to = std::min(to, lv.size());
+    for (size_t li = rest ? (size_t)sub_from : from; li < to; ++li) {
         const LevelDesc &d = lv[li];
         v.base = d.base;
         v.slots = d.slots;
@@ -653,6 +679,8 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             ctx->use_graphs = !(ng && ng[0] && ng[0] != '0');
             const char *np = std::getenv("ORB_NO_PDL");
             ctx->use_pdl = !(np && np[0] && np[0] != '0');
+            const char *ns = std::getenv("ORB_NO_STAGE");
+            ctx->use_stage = !(ns && ns[0] && ns[0] != '0');
         }
         if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess ||
             (e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_sub_flag), sizeof(uint32_t))) != cudaSuccess) {
@@ -682,6 +710,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->x.release(); ctx->y.release(); ctx->z.release();
+    ctx->yraw.release(); ctx->zraw.release();
     ctx->idx.release();
     ctx->heap.release(); ctx->ranges.release();
     ctx->tile_off.release(); ctx->hist_off.release(); ctx->below.release(); ctx->inb.release();
@@ -711,6 +740,7 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->yz_ready) cudaEventDestroy(ctx->yz_ready);
+    if (ctx->y_ready) cudaEventDestroy(ctx->y_ready);
     delete ctx;
     return ORB_OK;
 }
@@ -794,6 +824,23 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
     cudaStream_t s = ctx->stream;
     float h2d_ms = 0.f, d2h_ms = 0.f;
     ctx->yz_pending = false;
+    std::vector<LevelDesc> lv;
+    for (uint32_t l = 1; l <= levels; ++l)
+        lv.push_back({sl.first(l), nullptr, sl.count(l)});  // src/orbit.cpp:104-107
+    // subtrees finish complete unweighted trees only: d a power of two, built to its leaves
+    const int sub_from = subtree_from(ctx, lv, n, !weighted && sl.pow2 && levels == sl.depth);
+    if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
+    // Staged build from host memory: the copies of x, y and z follow one another, and the
+    // levels start as soon as the coordinates they read are on the device. Level 1 cuts along
+    // x (src/orbit.cpp:75), so it runs on x alone while y arrives; its swaps move x and the
+    // permutation, and y then takes the new order through the permutation. Level 2 cuts each
+    // cell along its longest side, whose y and z extents are the root box's and whose x
+    // extent is at most the root's: with y at least as long as z (and longer than zero), the
+    // first-longest rule of setCutAxis (src/cell.h:102-121) picks x or y there, so level 2
+    // runs on x and y while z arrives. Same cuts, same swaps: the result is the unstaged one.
+    const float y_ext = upper[1] - lower[1], z_ext = upper[2] - lower[2];
+    const bool staged = !dev && n && !weighted && ctx->use_stage && levels >= 2 &&
+                        (sub_from < 0 || sub_from >= 2) && y_ext > 0.f && y_ext >= z_ext;
     if (!dev) {
         ORB_CUDA(ctx->x.ensure(n + 1));
         ORB_CUDA(ctx->y.ensure(n + 1));
@@ -801,21 +848,36 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         dx = ctx->x.p;
         dy = ctx->y.p;
         dz = ctx->z.p;
+        if (staged) {
+            ORB_CUDA(ctx->yraw.ensure(n + 1));
+            ORB_CUDA(ctx->zraw.ensure(n + 1));
+        }
         ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
         if (n) {
             // x first; y and z on the copy stream, so the root level (cut along x,
             // src/orbit.cpp:75) bisects while they arrive; its partition waits for them
             if (!ctx->copy_stream) ORB_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
             if (!ctx->yz_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->yz_ready, cudaEventDisableTiming));
+            if (!ctx->y_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->y_ready, cudaEventDisableTiming));
             ORB_CUDA(cudaMemcpyAsync(dx, x, n * sizeof(float), cudaMemcpyHostToDevice, s));
             if (weighted)  // the root level's bisection reads x and the weights
                 ORB_CUDA(cudaMemcpyAsync(dw, w, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-            ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[2], 0));
-            ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
-            ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
+            if (staged) {  // one copy at a time, in the order the levels need them
+                ORB_CUDA(cudaEventRecord(ctx->y_ready, s));
+                ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->y_ready, 0));
+                ORB_CUDA(cudaMemcpyAsync(ctx->yraw.p, y, n * sizeof(float), cudaMemcpyHostToDevice,
+                                         ctx->copy_stream));
+                ORB_CUDA(cudaEventRecord(ctx->y_ready, ctx->copy_stream));
+                ORB_CUDA(cudaMemcpyAsync(ctx->zraw.p, z, n * sizeof(float), cudaMemcpyHostToDevice,
+                                         ctx->copy_stream));
+            } else {
+                ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[2], 0));
+                ORB_CUDA(cudaMemcpyAsync(dy, y, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
+                ORB_CUDA(cudaMemcpyAsync(dz, z, n * sizeof(float), cudaMemcpyHostToDevice, ctx->copy_stream));
+                ctx->yz_pending = true;
+            }
             ORB_CUDA(cudaEventRecord(ctx->yz_ready, ctx->copy_stream));
             ORB_CUDA(cudaEventRecord(ctx->ev[3], ctx->copy_stream));
-            ctx->yz_pending = true;
         } else {
             ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
         }
@@ -829,9 +891,6 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         v.wbelow = ctx->wbelow.p;
         v.wtot = ctx->wtot.p;
     }
-    std::vector<LevelDesc> lv;
-    for (uint32_t l = 1; l <= levels; ++l)
-        lv.push_back({sl.first(l), nullptr, sl.count(l)});  // src/orbit.cpp:104-107
     std::vector<uint64_t> key = level_key(ctx, v);
     key.push_back(0xB111D);  // single build
     key.push_back(n);
@@ -841,9 +900,6 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         key_add_f(key, lower[a]);
         key_add_f(key, upper[a]);
     }
-    // subtrees finish complete unweighted trees only: d a power of two, built to its leaves
-    const int sub_from = subtree_from(ctx, lv, n, !weighted && sl.pow2 && levels == sl.depth);
-    if (sub_from >= 0) ORB_CUDA(ctx->sub_flag.ensure(1));
     key.push_back((uint64_t)(int64_t)sub_from);
     // pinned host outputs of a build that plans subtrees: the subtree kernel writes every
     // finished cell straight into them (the transfer overlaps the last levels)
@@ -854,12 +910,35 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
     for (const void *p : {(const void *)v.hx, (const void *)v.hy, (const void *)v.hz, (const void *)v.hperm})
         key_add(key, p);
     key.push_back(ctx->yz_pending ? 1u : 0u);  // the graph waits for y and z before the first swap
+    key.push_back(staged ? 1u : 0u);
+    key_add(key, ctx->yraw.p);
+    key_add(key, ctx->zraw.p);
+    key_add(key, ctx->idx.p);
     uint32_t passes = 0;
     st = run_graphed(ctx, key, &passes, [&](uint32_t *pp) -> orb_status {
         ctx->launches[kKInit] += 1;
-        launch_init(v, n, lower, upper, d, (int)heap_cells, s);
+        if (!staged) {
+            launch_init(v, n, lower, upper, d, (int)heap_cells, s);
+            ORB_CUDA(cudaGetLastError());
+            return run_levels(ctx, v, lv, pp, sub_from, n);
+        }
+        const unsigned wf = ctx->capturing ? cudaEventWaitExternal : 0;
+        Level v1 = v;  // level 1: x and the permutation
+        v1.y = v1.z = nullptr;
+        v1.idx = ctx->idx.p;
+        launch_init(v1, n, lower, upper, d, (int)heap_cells, s);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp, sub_from, n);
+        orb_status ls = run_levels(ctx, v1, lv, pp, sub_from, n, false, 0, 1);
+        if (ls != ORB_OK) return ls;
+        ORB_CUDA(cudaStreamWaitEvent(s, ctx->y_ready, wf));
+        run_stage_gather(ctx, dy, ctx->yraw.p, n);
+        Level v2 = v1;  // level 2: x, y and the permutation
+        v2.y = dy;
+        if ((ls = run_levels(ctx, v2, lv, pp, sub_from, n, false, 1, 2)) != ORB_OK) return ls;
+        ORB_CUDA(cudaStreamWaitEvent(s, ctx->yz_ready, wf));
+        run_stage_gather(ctx, dz, ctx->zraw.p, n);
+        ORB_CUDA(cudaGetLastError());
+        return run_levels(ctx, v, lv, pp, sub_from, n, false, 2);  // the rest: everything
     });
     if (st != ORB_OK) return st;
     if (ctx->yz_pending || (!dev && n)) {

@@ -77,6 +77,7 @@ enum Kernel : int {
     kKWStart,
     kKWHist,
     kKWResolve,
+    kKStageGather,
     kNumKernels
 };
 static_assert(kNumKernels <= 32, "BuildCounters::bytes holds 32 kernel kinds");
@@ -289,6 +290,8 @@ cudaStream_t ctx_stream(orb_ctx *ctx);
 void ctx_disable_graphs(orb_ctx *ctx);
 void launch_iota_u32(uint32_t *dst, uint64_t n, cudaStream_t st);  // dst[p] = p
 // gather: dst[off+p] = src[off + perm[off+p]] for p < n (instance-relative permutation)
+void launch_stage_gather(float *dst, const float *src, const uint32_t *idx, uint64_t n,
+                         BuildCounters *ctr, int num_sms, cudaStream_t st);
 void launch_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
                        uint64_t n, cudaStream_t st);
 

@@ -30,7 +30,7 @@ const char *const kKernelNames[kNumKernels] = {
     "part_cells", "part_swap", "part_finish", "count_left", "generate", "bisect_cta",
     "tile_map", "bisect_tile", "warm_start", "subtree_check", "subtree",
     "count_left_sample", "count_left_sample_pick", "weighted_start", "count_left_weighted",
-    "bisect_resolve_weighted"};
+    "bisect_resolve_weighted", "stage_gather"};
 
 namespace {
 
@@ -2160,16 +2160,22 @@ __device__ __forceinline__ void emit_positions(const uint32_t *words, uint32_t r
     }
 }
 
+// (y or z null: that array is not moved at this level; builds from host memory reorder it
+// later through the permutation, see orb_build)
 __device__ __forceinline__ void swap_particles(const Level &v, uint32_t a, uint32_t b) {
     const float xa = v.x[a], xb = v.x[b];
-    const float ya = v.y[a], yb = v.y[b];
-    const float za = v.z[a], zb = v.z[b];
     v.x[a] = xb;
     v.x[b] = xa;
-    v.y[a] = yb;
-    v.y[b] = ya;
-    v.z[a] = zb;
-    v.z[b] = za;
+    if (v.y) {
+        const float ya = v.y[a], yb = v.y[b];
+        v.y[a] = yb;
+        v.y[b] = ya;
+    }
+    if (v.z) {
+        const float za = v.z[a], zb = v.z[b];
+        v.z[a] = zb;
+        v.z[b] = za;
+    }
     if (v.idx) {
         const uint32_t ia = v.idx[a], ib = v.idx[b];
         v.idx[a] = ib;
@@ -2211,7 +2217,10 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #ifndef ORB_SWAP_MIN_BLOCKS
 #define ORB_SWAP_MIN_BLOCKS 4
 #endif
-template <bool kWt>  // kWt: weighted builds, whose weights move with their particles
+// kWt: weighted builds, whose weights move with their particles. kYZ: bit 0 y moves, bit 1 z
+// moves (3 normally; the first levels of a build from host memory move x before y and z have
+// arrived, see orb_build).
+template <bool kWt, int kYZ>
 __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
@@ -2258,10 +2267,14 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                 if (ok) {
                     xa[q] = v.x[pa[q]];
                     xb[q] = v.x[pb[q]];
-                    ya[q] = v.y[pa[q]];
-                    yb[q] = v.y[pb[q]];
-                    za[q] = v.z[pa[q]];
-                    zb[q] = v.z[pb[q]];
+                    if constexpr ((kYZ & 1) != 0) {
+                        ya[q] = v.y[pa[q]];
+                        yb[q] = v.y[pb[q]];
+                    }
+                    if constexpr ((kYZ & 2) != 0) {
+                        za[q] = v.z[pa[q]];
+                        zb[q] = v.z[pb[q]];
+                    }
                     if (v.idx) {
                         ia[q] = v.idx[pa[q]];
                         ib[q] = v.idx[pb[q]];
@@ -2277,10 +2290,14 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
                 if (pa[q] == 0xffffffffu) continue;
                 v.x[pa[q]] = xb[q];
                 v.x[pb[q]] = xa[q];
-                v.y[pa[q]] = yb[q];
-                v.y[pb[q]] = ya[q];
-                v.z[pa[q]] = zb[q];
-                v.z[pb[q]] = za[q];
+                if constexpr ((kYZ & 1) != 0) {
+                    v.y[pa[q]] = yb[q];
+                    v.y[pb[q]] = ya[q];
+                }
+                if constexpr ((kYZ & 2) != 0) {
+                    v.z[pa[q]] = zb[q];
+                    v.z[pb[q]] = za[q];
+                }
                 if (v.idx) {
                     v.idx[pa[q]] = ib[q];
                     v.idx[pb[q]] = ia[q];
@@ -2296,7 +2313,8 @@ __global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Lev
     }
     // per pair: both elements of x, y, z (and idx, weights) read and written
     if (threadIdx.x == 0 && bytes)
-        add_bytes(v, kKPartSwap, (48ull + (v.idx ? 16ull : 0ull) + (kWt ? 16ull : 0ull)) * bytes);
+        add_bytes(v, kKPartSwap, (16ull * (1 + (kYZ & 1) + ((kYZ >> 1) & 1)) + (v.idx ? 16ull : 0ull) +
+                                  (kWt ? 16ull : 0ull)) * bytes);
 }
 
 __device__ void set_axis_and_margin(orb_cell_t &c, BuildCounters *ctr) {
@@ -3331,6 +3349,25 @@ __global__ void k_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t 
         dst[off + p] = src[off + perm[off + p]];
 }
 
+// Staged builds from host memory: a coordinate that arrived after the first levels moved the
+// other coordinates takes their order through the permutation, dst[p] = src[idx[p]].
+__global__ void __launch_bounds__(256) k_stage_gather(float *__restrict__ dst, const float *__restrict__ src,
+                                                      const uint32_t *__restrict__ idx, uint64_t n,
+                                                      BuildCounters *ctr) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t n4 = n / 4;  // dst and idx are 16-byte aligned allocations
+    const uint4 *idx4 = reinterpret_cast<const uint4 *>(idx);
+    float4 *dst4 = reinterpret_cast<float4 *>(dst);
+    for (uint64_t q = g; q < n4; q += stride) {
+        const uint4 i = idx4[q];
+        dst4[q] = make_float4(src[i.x], src[i.y], src[i.z], src[i.w]);
+    }
+    for (uint64_t p = n4 * 4 + g; p < n; p += stride) dst[p] = src[idx[p]];
+    // per particle: its index and the gathered value read, the value written
+    if (g == 0) atomicAdd(&ctr->bytes[kKStageGather], 12ull * n);
+}
+
 inline int grid_for(uint64_t n, int threads, int cap) {
     uint64_t g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -3414,9 +3451,13 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKPartCells: launch_kernel(p, k_part_cells, dim3(per_cell_warps), T, 0, st, v); break;
         case kKPartSwap:
             if (v.wt)
-                launch_kernel(p, k_part_swap<true>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<true, 3>, dim3(grid), T, 0, st, v);
+            else if (!v.y)
+                launch_kernel(p, k_part_swap<false, 0>, dim3(grid), T, 0, st, v);
+            else if (!v.z)
+                launch_kernel(p, k_part_swap<false, 1>, dim3(grid), T, 0, st, v);
             else
-                launch_kernel(p, k_part_swap<false>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<false, 3>, dim3(grid), T, 0, st, v);
             break;
         case kKWStart: launch_kernel(p, k_wstart, dim3(grid), T, 0, st, v); break;
         case kKWHist: launch_kernel(p, k_whist, dim3(grid), T, 0, st, v); break;
@@ -3457,6 +3498,11 @@ void launch_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n, 
 
 void launch_iota_u32(uint32_t *dst, uint64_t n, cudaStream_t st) {
     if (n) k_iota_u32<<<grid_for(n, 256, 152 * 16), 256, 0, st>>>(dst, n);
+}
+
+void launch_stage_gather(float *dst, const float *src, const uint32_t *idx, uint64_t n,
+                         BuildCounters *ctr, int num_sms, cudaStream_t st) {
+    if (n) k_stage_gather<<<grid_for((n + 3) / 4, 256, num_sms * 8), 256, 0, st>>>(dst, src, idx, n, ctr);
 }
 
 void launch_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t *perm, uint64_t off,
