@@ -17,6 +17,8 @@
 #include <list>
 #include <mutex>
 #include <new>
+#include <thread>
+#include <atomic>
 #include <string>
 #include <utility>
 #include <vector>
@@ -141,8 +143,12 @@ struct orb_ctx {
         uint32_t passes = 0;
     };
     std::list<Graph> graphs;
-    Graph *last_graph = nullptr;  // the graph of the last build (for its profile)
+    std::vector<Graph *> ran;  // graphs replayed since their profiles were last read
     static constexpr size_t kMaxGraphs = 256;
+    // window reports of the subtree kernel (builds from host memory): pinned and mapped
+    uint32_t e2e_windows = 16;  // ORB_E2E_WINDOWS (0: the particles are copied back after the build)
+    HostWindows *h_win = nullptr, *d_win = nullptr;
+    DevBuf<uint32_t> win_cnt;
 };
 
 namespace {
@@ -170,20 +176,6 @@ bool is_device_ptr(const void *p) {
         return false;
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
-// The device-accessible address of pinned (page-locked or registered) host memory; false for
-// any other pointer.
-template <class T>
-bool host_device_ptr(T *p, T **out) {
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
-    *out = static_cast<T *>(a.devicePointer);
-    return true;
 }
 
 orb_status ensure_ptile_buffers(orb_ctx *ctx, uint64_t ptiles) {
@@ -339,6 +331,7 @@ void collect_profile(orb_ctx *ctx) {
 }
 
 void drop_graph(orb_ctx *ctx, orb_ctx::Graph &g) {
+    ctx->ran.erase(std::remove(ctx->ran.begin(), ctx->ran.end(), &g), ctx->ran.end());
     if (g.exec) cudaGraphExecDestroy(g.exec);
     if (g.graph) cudaGraphDestroy(g.graph);
     for (auto &r : g.recs) {
@@ -351,16 +344,18 @@ void drop_graph(orb_ctx *ctx, orb_ctx::Graph &g) {
 void drop_all_graphs(orb_ctx *ctx) {
     for (auto &g : ctx->graphs) drop_graph(ctx, g);
     ctx->graphs.clear();
-    ctx->last_graph = nullptr;
+    ctx->ran.clear();
 }
 
-// Adds the event durations of the last replayed graph to the per-kernel totals.
+// Adds the event durations of the graphs replayed since the last call to the per-kernel
+// totals (their replays must have finished).
 void collect_graph_profile(orb_ctx *ctx) {
-    if (!ctx->last_graph) return;
-    for (auto &r : ctx->last_graph->recs) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.kind] += ms;
-    }
+    for (orb_ctx::Graph *g : ctx->ran)
+        for (auto &r : g->recs) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->prof_ms[r.kind] += ms;
+        }
+    ctx->ran.clear();
     cudaGetLastError();
 }
 
@@ -369,7 +364,6 @@ void collect_graph_profile(orb_ctx *ctx) {
 template <class Body>
 orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t *passes, Body &&body) {
     cudaStream_t s = ctx->stream;
-    ctx->last_graph = nullptr;
     if (!ctx->use_graphs) return body(passes);
     auto hit = ctx->graphs.begin();
     for (; hit != ctx->graphs.end(); ++hit)
@@ -423,7 +417,7 @@ orb_status run_graphed(orb_ctx *ctx, const std::vector<uint64_t> &key, uint32_t 
     ORB_CUDA(cudaGraphLaunch(g.exec, s));
     for (int k = 0; k < kNumKernels; ++k) ctx->launches[k] += g.launches[k];
     *passes += g.passes;
-    ctx->last_graph = &g;
+    if (std::find(ctx->ran.begin(), ctx->ran.end(), &g) == ctx->ran.end()) ctx->ran.push_back(&g);
     return ORB_OK;
 }
 
@@ -450,6 +444,7 @@ std::vector<uint64_t> level_key(orb_ctx *ctx, const Level &v) {
                           (const void *)v.whist, (const void *)v.wbelow, (const void *)v.wtot})
         key_add(key, p);
     key.push_back((uint64_t)ctx->pt_status.cap);
+    key_add(key, ctx->sub_flag.p);
     key.push_back(ctx->prof_mask);
     key.push_back(((uint64_t)ctx->spin_limit << 8) | ctx->scan_ticket_start);
     key.push_back(ctx->use_pdl ? 1u : 0u);
@@ -474,7 +469,7 @@ void partition_level(orb_ctx *ctx, const Level &v, bool do_split) {
         cudaStreamWaitEvent(ctx->stream, ctx->yz_ready, ctx->capturing ? cudaEventWaitExternal : 0);
         ctx->yz_pending = false;
     }
-    run_kernel(ctx, kKPartSwap, v, g);
+    run_kernel(ctx, kKPartSwap, v, ctx->num_sms * swap_blocks_per_sm());
     run_kernel(ctx, kKPartFinish, v, g, do_split ? 1 : 0);
 }
 
@@ -532,7 +527,7 @@ int subtree_from(const orb_ctx *ctx, const std::vector<LevelDesc> &lv, uint64_t 
 // rest = false: the levels above sub_from, then (sub_from >= 0) the subtree check and the
 // subtree kernel for the levels from sub_from down; rest = true: the levels from sub_from
 // down one by one, for builds whose subtree path the device refused.
-// [from, to): only those levels (staged builds run the levels in three pieces).
+// [from, to): only those levels (staged builds run the levels in pieces).
 orb_status run_levels(orb_ctx *ctx, Level v, const std::vector<LevelDesc> &lv, uint32_t *passes,
                       int sub_from, uint64_t max_n, bool rest = false, size_t from = 0,
                       size_t to = SIZE_MAX) {
@@ -681,9 +676,14 @@ orb_status orb_ctx_create(int device, const orb_opts *opts, orb_ctx **out) {
             ctx->use_pdl = !(np && np[0] && np[0] != '0');
             const char *ns = std::getenv("ORB_NO_STAGE");
             ctx->use_stage = !(ns && ns[0] && ns[0] != '0');
+            const char *ew = std::getenv("ORB_E2E_WINDOWS");
+            if (ew && ew[0]) ctx->e2e_windows = (uint32_t)std::min<long>(std::max<long>(0, std::atol(ew)), kMaxWindows);
         }
         if ((e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_counters), sizeof(BuildCounters))) != cudaSuccess ||
-            (e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_sub_flag), sizeof(uint32_t))) != cudaSuccess) {
+            (e = cudaMallocHost(reinterpret_cast<void **>(&ctx->h_sub_flag), sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaHostAlloc(reinterpret_cast<void **>(&ctx->h_win), sizeof(HostWindows), cudaHostAllocMapped)) !=
+                cudaSuccess ||
+            (e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&ctx->d_win), ctx->h_win, 0)) != cudaSuccess) {
             st = cuda_fail(ctx, e, "cudaMallocHost");
             break;
         }
@@ -732,6 +732,8 @@ orb_status orb_ctx_destroy(orb_ctx *ctx) {
     ctx->cmp_keys.release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->h_sub_flag) cudaFreeHost(ctx->h_sub_flag);
+    if (ctx->h_win) cudaFreeHost(ctx->h_win);
+    ctx->win_cnt.release();
     collect_profile(ctx);
     drop_all_graphs(ctx);
     for (auto e : ctx->ev_pool) cudaEventDestroy(e);
@@ -901,14 +903,24 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         key_add_f(key, upper[a]);
     }
     key.push_back((uint64_t)(int64_t)sub_from);
-    // pinned host outputs of a build that plans subtrees: the subtree kernel writes every
-    // finished cell straight into them (the transfer overlaps the last levels)
-    const bool direct = !dev && n && sub_from >= 0 && host_device_ptr(x, &v.hx) &&
-                        host_device_ptr(y, &v.hy) && host_device_ptr(z, &v.hz) &&
-                        (!perm || host_device_ptr(perm, &v.hperm));
-    if (!direct) v.hx = v.hy = v.hz = nullptr, v.hperm = nullptr;
-    for (const void *p : {(const void *)v.hx, (const void *)v.hy, (const void *)v.hz, (const void *)v.hperm})
-        key_add(key, p);
+    // window reports (builds from host memory that plan subtrees): the subtree kernel reports
+    // each window of consecutive root cells once all of them are final, and the host copies
+    // that window back while the kernel builds the next ones
+    const bool windows = !dev && n && !weighted && sub_from >= 0 && ctx->e2e_windows > 0;
+    uint32_t nwin = 0;
+    if (windows) {
+        ORB_CUDA(ctx->win_cnt.ensure(kMaxWindows));
+        const uint32_t cs = (uint32_t)lv[sub_from].C;
+        const uint32_t m = std::min<uint32_t>(ctx->e2e_windows, cs);
+        v.hwin = ctx->d_win;
+        v.win_cnt = ctx->win_cnt.p;
+        v.win_cells = (cs + m - 1) / m;
+        nwin = (cs + v.win_cells - 1) / v.win_cells;
+        std::memset(ctx->h_win, 0, sizeof(HostWindows));  // the device writes it during the build
+    }
+    key_add(key, v.hwin);
+    key_add(key, v.win_cnt);
+    key.push_back(v.win_cells);
     key.push_back(ctx->yz_pending ? 1u : 0u);  // the graph waits for y and z before the first swap
     key.push_back(staged ? 1u : 0u);
     key_add(key, ctx->yraw.p);
@@ -938,7 +950,7 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         ORB_CUDA(cudaStreamWaitEvent(s, ctx->yz_ready, wf));
         run_stage_gather(ctx, dz, ctx->zraw.p, n);
         ORB_CUDA(cudaGetLastError());
-        return run_levels(ctx, v, lv, pp, sub_from, n, false, 2);  // the rest: everything
+        return run_levels(ctx, v, lv, pp, sub_from, n, false, 2);  // the rest
     });
     if (st != ORB_OK) return st;
     if (ctx->yz_pending || (!dev && n)) {
@@ -946,16 +958,62 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         ctx->yz_pending = false;
         ORB_CUDA(cudaStreamWaitEvent(s, ctx->yz_ready, 0));
     }
+    // the windows: the host waits for each report (or for the build's end) and queues the
+    // window's copies back on the copy stream; *all: every window was reported
+    bool win_started = false;
+    auto stream_windows = [&](bool *all) -> orb_status {
+        *all = false;
+        HostWindows *hw = ctx->h_win;
+        auto wait_for = [&](volatile uint32_t *flag) -> bool {  // false: the build ended first
+            for (uint32_t it = 0;; ++it) {
+                if (*flag) return true;
+                if ((it & 31u) == 31u) {
+                    const cudaError_t q = cudaStreamQuery(s);
+                    if (q != cudaErrorNotReady) {
+                        cudaGetLastError();
+                        return *flag != 0;
+                    }
+                }
+                std::this_thread::yield();
+            }
+        };
+        if (!wait_for(&hw->decision) || hw->decision != 1u) return ORB_OK;
+        for (uint32_t w = 0; w < nwin; ++w) {
+            if (!wait_for(&hw->done[w])) return ORB_OK;
+            std::atomic_thread_fence(std::memory_order_acquire);
+            const volatile uint32_t *hr = &hw->range[w].x;
+            const uint2 r = make_uint2(hr[0], hr[1]);
+            cudaStream_t cs = ctx->copy_stream;
+            if (!win_started) {
+                // the copies in ended before the first window (the build waited for them)
+                ORB_CUDA(cudaEventSynchronize(ctx->ev[3]));
+                ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
+                ORB_CUDA(cudaEventRecord(ctx->ev[2], cs));
+                win_started = true;
+            }
+            if (r.y <= r.x || r.y > n) continue;
+            const size_t b = r.x, m = r.y - r.x;
+            ORB_CUDA(cudaMemcpyAsync(x + b, dx + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));
+            ORB_CUDA(cudaMemcpyAsync(y + b, dy + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));
+            ORB_CUDA(cudaMemcpyAsync(z + b, dz + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));
+            if (perm)
+                ORB_CUDA(cudaMemcpyAsync(perm + b, ctx->idx.p + b, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs));
+        }
+        *all = true;
+        return ORB_OK;
+    };
     ORB_CUDA(cudaEventRecord(ctx->ev[1], s));
+    bool streamed = false;
+    if (windows && (st = stream_windows(&streamed)) != ORB_OK) return st;
     bool taken = false;  // the subtree kernel finished the tree
     st = finish_subtree_levels(ctx, v, lv, key, &passes, sub_from, n, &taken);
     if (st != ORB_OK) return st;
-    bool written = false;  // the subtree kernel wrote the particles to the host arrays
+    bool written = false;  // the particles are in the host arrays (or on their way there)
     if (!dev) {
         ORB_CUDA(cudaStreamSynchronize(s));
-        ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
-        written = direct && taken;
-        ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
+        if (!win_started) ORB_CUDA(cudaEventElapsedTime(&h2d_ms, ctx->ev[2], ctx->ev[3]));
+        written = streamed && taken;
+        if (!win_started) ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
         if (n && !written) {
             ORB_CUDA(cudaMemcpyAsync(x, dx, n * sizeof(float), cudaMemcpyDeviceToHost, s));
             ORB_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -970,8 +1028,14 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
     ORB_CUDA(cudaMemcpyAsync(heap, ctx->heap.p, heap_cells * sizeof(orb_cell_t), cudaMemcpyDeviceToHost, s));
     ORB_CUDA(cudaMemcpyAsync(ranges, ctx->ranges.p, heap_cells * sizeof(uint2), cudaMemcpyDeviceToHost, s));
     ORB_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->counters.p, sizeof(BuildCounters), cudaMemcpyDeviceToHost, s));
-    if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+    const bool on_cs = win_started;  // copies back on the copy stream
+    if (on_cs && !written) {  // and some on the context stream after them: both timed
+        ORB_CUDA(cudaEventRecord(ctx->ev[3], s));
+        ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[3], 0));
+    }
+    if (!dev) ORB_CUDA(cudaEventRecord(ctx->ev[3], on_cs ? ctx->copy_stream : s));
     ORB_CUDA(cudaStreamSynchronize(s));
+    if (on_cs) ORB_CUDA(cudaStreamSynchronize(ctx->copy_stream));
     if (ctx->h_counters->error)
         return fail(ctx, ORB_ERR_TIMEOUT, "a bounded device wait gave up or a bisection did not finish");
     float dev_ms = 0.f;

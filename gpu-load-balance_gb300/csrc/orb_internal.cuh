@@ -100,6 +100,17 @@ struct BuildCounters {
     unsigned long long bytes[32];  // algorithmic bytes per Kernel kind
 };
 
+// Builds from host memory: the subtree kernel reports, per window of consecutive root cells,
+// when every cell of the window is final, into pinned host memory that the host polls while
+// the kernel runs; the host then copies the window's particles back while later windows are
+// still being built.
+constexpr int kMaxWindows = 64;
+struct HostWindows {
+    uint32_t decision;           // 0 not yet, 1 the subtree kernel finishes the tree, 2 refused
+    uint32_t done[kMaxWindows];  // 1: window w final, its particles in range[w]
+    uint2 range[kMaxWindows];
+};
+
 // Everything a level's kernels need. Cells of the level are heap slots [base, base + C)
 // unless `slots` is non-null (service calls over an arbitrary cell list).
 struct Level {
@@ -160,11 +171,11 @@ struct Level {
     // subtrees: 1 when one CTA per cell finishes the tree from this level down (then the
     // level kernels of the levels below return at once); null when not attempted
     uint32_t *skip;
-    // single builds from pinned host arrays (null otherwise): device-accessible addresses of
-    // the caller's x, y, z (and permutation) arrays; the subtree kernel writes each finished
-    // cell's final particles there, overlapping the device-to-host transfer with the last levels
-    float *hx, *hy, *hz;
-    uint32_t *hperm;
+    // window reports (null otherwise): the host-mapped reports, a finished-cell counter per
+    // window, root cells per window
+    HostWindows *hwin;
+    uint32_t *win_cnt;
+    uint32_t win_cells;
     // weighted builds (null otherwise): an integer weight per particle, moved with it, and
     // per cell of the level its weight bins (kWBins), the weight below its bracket and its
     // total weight
@@ -277,6 +288,7 @@ void launch_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *
 void launch_displace(float *x, float *y, float *z, uint64_t offset, uint64_t n, uint64_t seed,
                      float sigma, const float lower[3], const float upper[3], cudaStream_t st);
 cudaError_t configure_kernels();  // once per device (dynamic shared memory limits)
+int swap_blocks_per_sm();         // resident CTAs of the swap kernel per SM (its grid)
 void launch_gen_uniform(uint64_t seed, uint64_t n, float *x, float *y, float *z,
                         cudaStream_t st);
 // `draws` draws of the reference's xorshf96 stream, thread g from starts[3g..3g+2] for `chunk`

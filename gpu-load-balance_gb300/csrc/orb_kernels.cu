@@ -2217,11 +2217,16 @@ __device__ __forceinline__ uint32_t warp_last_at_most(const uint32_t *pre, uint3
 #ifndef ORB_SWAP_MIN_BLOCKS
 #define ORB_SWAP_MIN_BLOCKS 4
 #endif
+#ifndef ORB_SWAP_THREADS
+#define ORB_SWAP_THREADS 256  // threads of a swap CTA (at least kPWords: one mask word each)
+#endif
+constexpr int kSwapThreads = ORB_SWAP_THREADS;
+static_assert(kSwapThreads >= kPWords && kSwapThreads % 32 == 0, "a swap CTA scans a tile's mask words");
 // kWt: weighted builds, whose weights move with their particles. kYZ: bit 0 y moves, bit 1 z
 // moves (3 normally; the first levels of a build from host memory move x before y and z have
 // arrived, see orb_build).
 template <bool kWt, int kYZ>
-__global__ void __launch_bounds__(kThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
+__global__ void __launch_bounds__(kSwapThreads, ORB_SWAP_MIN_BLOCKS) k_part_swap(Level v) {
     pdl_enter();
     if (v.skip && *(volatile const uint32_t *)v.skip) return;  // subtrees took this level
     if (scan_failed(v)) return;  // a look-back wait gave up: the prefixes are not valid
@@ -2926,33 +2931,21 @@ __global__ void __launch_bounds__(1024) k_subtree_check(Level v, int max_levels)
     }
     mx = block_max(mx, sh);
     ml = block_max(ml, sh);
-    if (threadIdx.x == 0)
-        *v.skip = mx <= kSubMax && (int)ml <= min(max_levels, kSubLevels) ? 1u : 0u;
-}
-
-// dst[i] = src[i] for i in [b, e) by the CTA (dst: host memory reached over the C2C link):
-// 16-byte stores when both arrays have the same alignment, else 4-byte ones.
-template <class T>
-__device__ void copy_out(const T *src, T *dst, uint32_t b, uint32_t e) {
-    static_assert(sizeof(T) == 4, "4-byte elements");
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uintptr_t sa = reinterpret_cast<uintptr_t>(src + b), da = reinterpret_cast<uintptr_t>(dst + b);
-    uint32_t a0 = b;
-    if (((sa ^ da) & 15u) == 0) {
-        a0 = min(e, b + (uint32_t)(((16u - (sa & 15u)) & 15u) >> 2));
-        const uint32_t n4 = (e - a0) >> 2;
-        const uint4 *s4 = reinterpret_cast<const uint4 *>(src + a0);
-        uint4 *d4 = reinterpret_cast<uint4 *>(dst + a0);
-        for (uint32_t j = tid; j < n4; j += nt) d4[j] = s4[j];
-        for (uint32_t i = b + tid; i < a0; i += nt) dst[i] = src[i];
-        for (uint32_t i = a0 + (n4 << 2) + tid; i < e; i += nt) dst[i] = src[i];
-    } else {
-        for (uint32_t i = b + tid; i < e; i += nt) dst[i] = src[i];
+    if (v.win_cnt)
+        for (int w = threadIdx.x; w < kMaxWindows; w += blockDim.x) v.win_cnt[w] = 0u;
+    if (threadIdx.x == 0) {
+        const uint32_t take = mx <= kSubMax && (int)ml <= min(max_levels, kSubLevels) ? 1u : 0u;
+        *v.skip = take;
+        v.counters->sub_next = 0u;  // the subtree kernel's work queue starts at the level's first cell
+        if (v.hwin) {
+            __threadfence_system();
+            *(volatile uint32_t *)&v.hwin->decision = take ? 1u : 2u;
+        }
     }
 }
 
 // One CTA per cell of the level: every level below it (its leaf count's log2), breadth
-// first; with host outputs (v.hx), the finished cell's particles are then written there.
+// first; with window reports (v.hwin), the last cell of each window reports it to the host.
 // kWarpSmall: cells of at most kWarpKeys particles go to one warp each (the CTA's warps side
 // by side); without it every cell is the whole CTA's (the instance for trees whose cells
 // never get that small keeps its registers for the CTA path). Same results either way.
@@ -3014,12 +3007,25 @@ __global__ void __launch_bounds__(kSubThreads, 4) k_subtree(Level v) {
             cur ^= 1;
             nq = 2 * nq;
         }
-        if (v.hx) {  // the cell's particles are final: to the caller's host arrays
-            const uint2 rg = v.ranges[root];
-            copy_out(v.x, v.hx, rg.x, rg.y);
-            copy_out(v.y, v.hy, rg.x, rg.y);
-            copy_out(v.z, v.hz, rg.x, rg.y);
-            if (v.hperm && v.idx) copy_out(v.idx, v.hperm, rg.x, rg.y);
+        if (v.hwin) {
+            // the cell is final: every thread's writes made visible beyond the GPU, then the
+            // last cell of its window reports the window's particle range to the host
+            __threadfence_system();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const uint32_t w = (uint32_t)c / v.win_cells;
+                const uint32_t first = w * v.win_cells, last = min(first + v.win_cells, (uint32_t)v.C) - 1u;
+                if (atomicAdd(&v.win_cnt[w], 1u) == last - first) {
+                    __threadfence_system();
+                    const uint2 r = make_uint2(v.ranges[level_slot(v, (int)first)].x,
+                                               v.ranges[level_slot(v, (int)last)].y);
+                    volatile uint32_t *hr = &v.hwin->range[w].x;
+                    hr[0] = r.x;
+                    hr[1] = r.y;
+                    __threadfence_system();
+                    *(volatile uint32_t *)&v.hwin->done[w] = 1u;
+                }
+            }
         }
     }
     // lane 0 of every warp counted the small cells its warp finished (thread 0 the rest too)
@@ -3359,7 +3365,16 @@ __global__ void __launch_bounds__(256) k_stage_gather(float *__restrict__ dst, c
     const uint64_t n4 = n / 4;  // dst and idx are 16-byte aligned allocations
     const uint4 *idx4 = reinterpret_cast<const uint4 *>(idx);
     float4 *dst4 = reinterpret_cast<float4 *>(dst);
-    for (uint64_t q = g; q < n4; q += stride) {
+    // two quads per thread and step: both index loads, then all eight gathers, in flight
+    uint64_t q = g;
+    for (; q + stride < n4; q += 2 * stride) {
+        const uint4 i = idx4[q], j = idx4[q + stride];
+        const float4 a = make_float4(src[i.x], src[i.y], src[i.z], src[i.w]);
+        const float4 b = make_float4(src[j.x], src[j.y], src[j.z], src[j.w]);
+        dst4[q] = a;
+        dst4[q + stride] = b;
+    }
+    if (q < n4) {
         const uint4 i = idx4[q];
         dst4[q] = make_float4(src[i.x], src[i.y], src[i.z], src[i.w]);
     }
@@ -3451,13 +3466,13 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
         case kKPartCells: launch_kernel(p, k_part_cells, dim3(per_cell_warps), T, 0, st, v); break;
         case kKPartSwap:
             if (v.wt)
-                launch_kernel(p, k_part_swap<true, 3>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<true, 3>, dim3(grid), dim3(kSwapThreads), 0, st, v);
             else if (!v.y)
-                launch_kernel(p, k_part_swap<false, 0>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<false, 0>, dim3(grid), dim3(kSwapThreads), 0, st, v);
             else if (!v.z)
-                launch_kernel(p, k_part_swap<false, 1>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<false, 1>, dim3(grid), dim3(kSwapThreads), 0, st, v);
             else
-                launch_kernel(p, k_part_swap<false, 3>, dim3(grid), T, 0, st, v);
+                launch_kernel(p, k_part_swap<false, 3>, dim3(grid), dim3(kSwapThreads), 0, st, v);
             break;
         case kKWStart: launch_kernel(p, k_wstart, dim3(grid), T, 0, st, v); break;
         case kKWHist: launch_kernel(p, k_whist, dim3(grid), T, 0, st, v); break;
@@ -3480,6 +3495,21 @@ void launch_level_kernel(Kernel k, const Level &v, int grid, int arg, cudaStream
 cudaError_t configure_kernels() {
     return cudaFuncSetAttribute(k_bisect_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kCtaSmemBytes);
+}
+
+int swap_blocks_per_sm() {
+    // the swap's CTAs walk the tiles grid-stride: one resident wave, none waiting behind it
+    static int blocks = 0;
+    if (!blocks) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_part_swap<false, 3>, kSwapThreads, 0) != cudaSuccess ||
+            b < 1) {
+            cudaGetLastError();
+            b = ORB_SWAP_MIN_BLOCKS;
+        }
+        blocks = b;
+    }
+    return blocks;
 }
 
 void launch_copy_instances(const uint32_t *src, uint32_t *dst, const BatchRoot *roots, int k,

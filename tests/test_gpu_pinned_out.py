@@ -1,7 +1,8 @@
 """Builds from pinned host arrays: when the build finishes its last levels in subtree CTAs,
-each CTA writes its cell's final particles (and permutation) straight into the caller's
-pinned arrays instead of a copy after the build. Results must be bit-identical to the
-oracle, whether the device takes the subtree path or refuses it (then the host copies)."""
+the subtree kernel reports each window of finished root cells and the host copies it back
+into the caller's pinned arrays while later windows are built. Results must be bit-identical
+to the oracle, whether the device takes the subtree path or refuses it (then the host copies
+everything after the level kernels finish the tree)."""
 import numpy as np
 import pytest
 

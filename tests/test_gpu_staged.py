@@ -80,3 +80,89 @@ def test_staged_equals_device_build(ctx, oracle):
     assert np.array_equal(res_h.perm, perm.cpu().numpy().view(np.uint32))
     for got, want in ((hx, dx), (hy, dy), (hz, dz)):
         assert np.array_equal(got.view(np.uint32), want.cpu().numpy().view(np.uint32))
+
+
+# Builds from host arrays that finish their last levels in subtree CTAs copy the particles
+# back in windows of consecutive root cells: the subtree kernel reports each window to the
+# host once every cell of it is final, and the host copies it back while the kernel builds the
+# next ones (16 windows by default; ORB_E2E_WINDOWS=0 copies everything after the build).
+
+def context_with_windows(engine, k):
+    import os
+    old = os.environ.get("ORB_E2E_WINDOWS")
+    os.environ["ORB_E2E_WINDOWS"] = str(k)
+    try:
+        return engine.Context(0)
+    finally:
+        if old is None:
+            del os.environ["ORB_E2E_WINDOWS"]
+        else:
+            os.environ["ORB_E2E_WINDOWS"] = old
+
+
+def pinned(a):
+    t = torch.empty(a.shape[0], dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
+                    pin_memory=True)
+    v = t.numpy().view(a.dtype)
+    v[:] = a
+    return t, v
+
+
+def check_host_build(c, oracle, x, y, z, d, use_pinned):
+    n = x.shape[0]
+    ref = oracle.build_tree(x, y, z, d, threads=8)
+    keep = []
+    if use_pinned:
+        arrs = []
+        for a in (x, y, z, np.zeros(n, np.uint32)):
+            t, v = pinned(a)
+            keep.append(t)
+            arrs.append(v)
+        hx, hy, hz, perm = arrs
+    else:
+        hx, hy, hz = (np.array(a, copy=True) for a in (x, y, z))
+        perm = np.zeros(n, np.uint32)
+    res = c.build(hx, hy, hz, d, perm=perm)
+    assert res.heap.tobytes() == ref.heap.tobytes()
+    assert np.array_equal(res.ranges, ref.ranges[0])
+    assert np.array_equal(perm, ref.perm)
+    for got, want in ((hx, ref.x), (hy, ref.y), (hz, ref.z)):
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    return res
+
+
+@pytest.mark.parametrize("kind,seed,n,d,use_pinned", [
+    ("uniform", 310, (1 << 22) + 12345, 1 << 12, False),
+    ("plummer", 311, 1 << 22, 1 << 14, True),
+    ("uniform", 312, 1 << 23, 1 << 16, True),
+    ("plummer", 315, 1 << 20, 1 << 10, True),
+])
+def test_windowed_host_build(ctx, oracle, kind, seed, n, d, use_pinned):
+    gen = oracle.gen_uniform if kind == "uniform" else oracle.gen_plummer
+    x, y, z = gen(seed, n)
+    check_host_build(ctx, oracle, x, y, z, d, use_pinned)
+
+
+@pytest.mark.parametrize("use_pinned", [False, True])
+def test_windowed_subtree_refused(ctx, oracle, use_pinned):
+    # a quarter of the particles on one point: a cell too large for one CTA remains at the
+    # subtree level, so the device refuses the subtree path, reports no window, and the level
+    # kernels finish the tree before everything is copied back
+    n, d = 1 << 22, 1 << 12
+    x, y, z = oracle.gen_uniform(313, n)
+    for a in (x, y, z):
+        a[: n // 4] = np.float32(0.3)
+    res = check_host_build(ctx, oracle, x, y, z, d, use_pinned)
+    assert res.info["degenerate_cells"] > 0 or res.info["unfound_cells"] > 0
+
+
+def test_window_counts_agree(engine, oracle):
+    # no windows, one, 8 and 64: the same tree and particle order
+    x, y, z = oracle.gen_plummer(314, 1 << 22)
+    d = 1 << 13
+    for k in (0, 1, 8, 64):
+        c = context_with_windows(engine, k)
+        try:
+            check_host_build(c, oracle, x, y, z, d, use_pinned=k % 2 == 0)
+        finally:
+            c.close()
