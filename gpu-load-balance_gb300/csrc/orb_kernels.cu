@@ -3073,7 +3073,7 @@ __global__ void __launch_bounds__(kThreads) k_whist(Level v) {
     __shared__ unsigned long long s_bins[kWBins];
     __shared__ unsigned long long s_red[kThreads / 32];
     const uint32_t total = v.tile_off[v.C];
-    unsigned long long bytes = 0;
+    unsigned long long bytes = 0, wkeys = 0;  // this thread's bracket weight reads; the CTA's keys
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const TileRef tr = tile_ref(v, t);
         if (v.state[tr.c] != kActive) continue;  // block-uniform
@@ -3083,29 +3083,58 @@ __global__ void __launch_bounds__(kThreads) k_whist(Level v) {
         for (uint32_t j = threadIdx.x; j < (uint32_t)kWBins; j += blockDim.x) s_bins[j] = 0ull;
         __syncthreads();
         unsigned long long below = 0, tot = 0;
-        for (uint32_t p = tr.e0 + threadIdx.x; p < tr.e1; p += blockDim.x) {
-            const float k = __ldg(keys + p);
-            const uint32_t w = __ldg(v.wt + p);
-            tot += w;
-            if (k < L)
-                below += w;
-            else if (k < R && w)
-                atomicAdd(&s_bins[tree_bin(k, L, R, kWBinsLog2)], (unsigned long long)w);
+        // kWLoads keys of a thread in flight per round. The first pass reads every weight
+        // (the cell's total and the weight below its bracket); later passes read the weights
+        // of the keys inside the bracket only (the weight below it is carried by k_wresolve).
+        constexpr int kWLoads = 4;
+        const uint32_t nt = blockDim.x;
+        const bool first = v.pass == 0;
+        for (uint32_t p0 = tr.e0 + threadIdx.x; p0 < tr.e1; p0 += nt * kWLoads) {
+            float k[kWLoads];
+            uint32_t w[kWLoads];
+#pragma unroll
+            for (int u = 0; u < kWLoads; ++u) {
+                const uint32_t p = p0 + (uint32_t)u * nt;
+                k[u] = p < tr.e1 ? __ldg(keys + p) : L;
+                w[u] = first && p < tr.e1 ? __ldg(v.wt + p) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < kWLoads; ++u) {
+                const uint32_t p = p0 + (uint32_t)u * nt;
+                if (p >= tr.e1) continue;
+                if (first) {
+                    tot += w[u];
+                    if (k[u] < L) below += w[u];
+                }
+                if (k[u] >= L && k[u] < R) {
+                    const uint32_t wk = first ? w[u] : __ldg(v.wt + p);
+                    if (wk) atomicAdd(&s_bins[tree_bin(k[u], L, R, kWBinsLog2)], (unsigned long long)wk);
+                    if (!first) ++bytes;  // a weight read (counted in 4-byte units below)
+                }
+            }
         }
-        below = block_sum_u64(below, s_red);
-        tot = block_sum_u64(tot, s_red);
+        if (first) {
+            below = block_sum_u64(below, s_red);
+            tot = block_sum_u64(tot, s_red);
+        }
         __syncthreads();
         unsigned long long *g = v.whist + (size_t)tr.c * kWBins;
         for (uint32_t j = threadIdx.x; j < (uint32_t)kWBins; j += blockDim.x)
             if (s_bins[j]) atomicAdd(&g[j], s_bins[j]);
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && first) {
             if (below) atomicAdd(&v.wbelow[tr.c], below);
-            if (v.pass == 0 && tot) atomicAdd(&v.wtot[tr.c], tot);
-            bytes += 8ull * (tr.e1 - tr.e0);
+            if (tot) atomicAdd(&v.wtot[tr.c], tot);
         }
+        if (threadIdx.x == 0) wkeys += tr.e1 - tr.e0;
         __syncthreads();  // s_bins reused by the next tile
     }
-    if (threadIdx.x == 0 && bytes) add_bytes(v, kKWHist, bytes);
+    // 4 B per key read (every pass), 4 B per weight read (every key in the first pass, the
+    // bracket's keys after it): per thread in-bracket weight reads summed over the block
+    const unsigned long long wr = v.pass == 0 ? 0ull : block_sum_u64(bytes, s_red);
+    if (threadIdx.x == 0) {
+        const unsigned long long b = 4ull * wkeys * (v.pass == 0 ? 2ull : 1ull) + 4ull * wr;
+        if (b) add_bytes(v, kKWHist, b);
+    }
 }
 
 // A warp per cell: the replay of up to kWBinsLog2 iterations of src/orbit.cpp:146-232 on the
@@ -3179,7 +3208,8 @@ __global__ void __launch_bounds__(kThreads) k_wresolve(Level v) {
         cell.foundCut = st == kFound ? 1 : 0;
         v.iters[c] = (uint8_t)it;
         v.state[c] = st;
-        v.wbelow[c] = 0ull;
+        // the weight below the new bracket [L, R): below the old one plus the bins left of it
+        v.wbelow[c] = below + pre[pos];
         if (st != kActive) atomicMax(&v.counters->max_iters, it);
         if (st == kCapped) atomicAdd(&v.counters->unfound, 1u);
     }
