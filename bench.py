@@ -579,7 +579,7 @@ def bench_weighted(ctx, E, torch, dev, args, n: int, d: int, seed: int, peak: fl
         "particles_per_s": n / (statistics.median(ms) / 1e3),
         "count_left_weighted": {"achieved": round(gbs, 1) if gbs else None, "unit": "GB/s",
                                 "frac": round(gbs / peak, 4) if gbs else None,
-                                "bytes": "8 B per key and pass (key + weight)"},
+                                "bytes": "4 B per key and pass, 4 B per weight read (every weight in the first pass, the bracket keys' after it)"},
         "leaf_weight_spread": round(float((sums.max() - sums.min()) / sums.mean()), 5),
         "kernels_per_step_warmup": kernels,
         "note": "labelled mode (the reference never implemented weighted ORB): every level "
