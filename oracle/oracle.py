@@ -49,6 +49,7 @@ class _Stats(ctypes.Structure):
         ("t_count_s", ctypes.c_double),
         ("t_partition_s", ctypes.c_double),
         ("t_total_s", ctypes.c_double),
+        ("elements_per_level", ctypes.c_uint64 * MAX_LEVELS),
     ]
 
 
@@ -228,6 +229,7 @@ def build_tree(x, y, z, d: int, levels: int | None = None, lower=(-0.5, -0.5, -0
         "iterations": list(st.iterations[: st.levels_built]),
         "cell_counts": st.cell_counts,
         "elements_counted": st.elements_counted,
+        "elements_per_level": list(st.elements_per_level[: st.levels_built]),
         "degenerate_cells": st.degenerate_cells,
         "zero_volume_cells": st.zero_volume_cells,
         "unfound_cells": st.unfound_cells,

@@ -556,6 +556,7 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
                 jmax = std::max(jmax, jdone[c]);
                 st.cell_counts += jdone[c];
                 st.elements_counted += counted[c];
+                st.elements_per_level[l - 1] += counted[c];
             }
             // the level loop of orbit.cpp:148 runs until every cell is found or 32 sweeps
             st.iterations[l - 1] = jmax;
@@ -593,6 +594,7 @@ int oracle_build(float *x, float *y, float *z, uint64_t n, uint32_t d, uint32_t 
                     if (cell.foundCut) continue;
                     ++st.cell_counts;
                     st.elements_counted += counts[c];
+                    st.elements_per_level[l - 1] += counts[c];
                     if (iters) iters[cell.id] = (uint8_t)j;
                     int dir = convergence(counts_left[c], counts[c], cell.nLeafCells, nullptr);
                     if (dir == 0) {

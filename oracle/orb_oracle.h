@@ -63,6 +63,7 @@ typedef struct oracle_stats {
     double t_count_s;
     double t_partition_s;
     double t_total_s;
+    uint64_t elements_per_level[ORACLE_MAX_LEVELS]; /* elements_counted by level */
 } oracle_stats_t;
 
 /* Seeded generators shared bit-for-bit with the engine's device generator. */
