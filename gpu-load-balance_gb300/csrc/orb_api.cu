@@ -991,8 +991,9 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
                 ORB_CUDA(cudaEventRecord(ctx->ev[2], cs));
                 win_started = true;
             }
-            if (r.y <= r.x || r.y > n) continue;
+            if (r.y < r.x || r.y > n) return ORB_OK;  // not a range of this build: copy all after it
             const size_t b = r.x, m = r.y - r.x;
+            if (!m) continue;
             ORB_CUDA(cudaMemcpyAsync(x + b, dx + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));
             ORB_CUDA(cudaMemcpyAsync(y + b, dy + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));
             ORB_CUDA(cudaMemcpyAsync(z + b, dz + b, m * sizeof(float), cudaMemcpyDeviceToHost, cs));

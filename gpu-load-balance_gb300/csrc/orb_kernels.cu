@@ -3529,16 +3529,15 @@ cudaError_t configure_kernels() {
 
 int swap_blocks_per_sm() {
     // the swap's CTAs walk the tiles grid-stride: one resident wave, none waiting behind it
-    static int blocks = 0;
-    if (!blocks) {
+    static const int blocks = [] {
         int b = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_part_swap<false, 3>, kSwapThreads, 0) != cudaSuccess ||
             b < 1) {
             cudaGetLastError();
             b = ORB_SWAP_MIN_BLOCKS;
         }
-        blocks = b;
-    }
+        return b;
+    }();
     return blocks;
 }
 
