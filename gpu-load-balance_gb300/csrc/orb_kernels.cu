@@ -3385,6 +3385,9 @@ __global__ void k_gather_u32(uint32_t *dst, const uint32_t *src, const uint32_t 
         dst[off + p] = src[off + perm[off + p]];
 }
 
+#ifndef ORB_GATHER_QUADS
+#define ORB_GATHER_QUADS 4  // quads of a thread in flight in the stage gather
+#endif
 // Staged builds from host memory: a coordinate that arrived after the first levels moved the
 // other coordinates takes their order through the permutation, dst[p] = src[idx[p]].
 __global__ void __launch_bounds__(256) k_stage_gather(float *__restrict__ dst, const float *__restrict__ src,
@@ -3395,16 +3398,20 @@ __global__ void __launch_bounds__(256) k_stage_gather(float *__restrict__ dst, c
     const uint64_t n4 = n / 4;  // dst and idx are 16-byte aligned allocations
     const uint4 *idx4 = reinterpret_cast<const uint4 *>(idx);
     float4 *dst4 = reinterpret_cast<float4 *>(dst);
-    // two quads per thread and step: both index loads, then all eight gathers, in flight
+    // kQ quads per thread and step: all index loads, then all 4 kQ gathers, in flight
+    constexpr int kQ = ORB_GATHER_QUADS;
     uint64_t q = g;
-    for (; q + stride < n4; q += 2 * stride) {
-        const uint4 i = idx4[q], j = idx4[q + stride];
-        const float4 a = make_float4(src[i.x], src[i.y], src[i.z], src[i.w]);
-        const float4 b = make_float4(src[j.x], src[j.y], src[j.z], src[j.w]);
-        dst4[q] = a;
-        dst4[q + stride] = b;
+    for (; q + (kQ - 1) * stride < n4; q += kQ * stride) {
+        uint4 i[kQ];
+#pragma unroll
+        for (int u = 0; u < kQ; ++u) i[u] = idx4[q + u * stride];
+        float4 a[kQ];
+#pragma unroll
+        for (int u = 0; u < kQ; ++u) a[u] = make_float4(src[i[u].x], src[i[u].y], src[i[u].z], src[i[u].w]);
+#pragma unroll
+        for (int u = 0; u < kQ; ++u) dst4[q + u * stride] = a[u];
     }
-    if (q < n4) {
+    for (; q < n4; q += stride) {
         const uint4 i = idx4[q];
         dst4[q] = make_float4(src[i.x], src[i.y], src[i.z], src[i.w]);
     }
