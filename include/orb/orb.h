@@ -123,6 +123,11 @@ int orb_abi_version(void);
  *   flags     ORB_DEVICE_POINTERS: x,y,z,perm are device pointers (heap/ranges stay host)
  *   info      out, optional
  * n must be below 2^31 (the reference's int indices).
+ * From host arrays the copies overlap the build: x, y and z are copied in one after another
+ * and each level starts once the coordinates it reads have arrived (when the box's y side is
+ * at least as long as its z side), and the particles are copied back in windows while the
+ * last levels are still being built. Page-locked (pinned) arrays make both copies faster. A
+ * call that fails waits for its copies before it returns.
  */
 orb_status orb_build(orb_ctx *ctx, float *x, float *y, float *z, uint64_t n, uint32_t d,
                      uint32_t levels, const float lower[3], const float upper[3],
