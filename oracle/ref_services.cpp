@@ -33,7 +33,7 @@
 static_assert(sizeof(Cell) == 52, "the reference's Cell is the 52-byte heap record");
 
 // MDL's traversal (src/services/TraversePST.cpp) walks the PST tree and calls Service() on
-// each leaf; here the driver calls every rank's Service() and Combine() itself, so the
+// each leaf; here refsvc_build below calls every rank's Service() and Combine() itself, so the
 // traversal entry points only forward to the leaf.
 int TraversePST::operator()(int nIn, void *pIn, void *pOut) {
     return Traverse(node_pst, pIn, nIn, pOut, getMaxBytesOut());
