@@ -856,8 +856,9 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
         }
         ORB_CUDA(cudaEventRecord(ctx->ev[2], s));
         if (n) {
-            // x first; y and z on the copy stream, so the root level (cut along x,
-            // src/orbit.cpp:75) bisects while they arrive; its partition waits for them
+            // x first on the build stream, y and z on the copy stream: a staged build copies
+            // them one after another; otherwise they cross together while the root level (cut
+            // along x, src/orbit.cpp:75) bisects, and its partition waits for them
             if (!ctx->copy_stream) ORB_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
             if (!ctx->yz_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->yz_ready, cudaEventDisableTiming));
             if (!ctx->y_ready) ORB_CUDA(cudaEventCreateWithFlags(&ctx->y_ready, cudaEventDisableTiming));
@@ -865,6 +866,7 @@ static orb_status build_single(orb_ctx *ctx, float *x, float *y, float *z, uint3
             if (weighted)  // the root level's bisection reads x and the weights
                 ORB_CUDA(cudaMemcpyAsync(dw, w, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
             if (staged) {  // one copy at a time, in the order the levels need them
+                // y_ready marks the end of x's copy (the copy stream waits for it), then y's
                 ORB_CUDA(cudaEventRecord(ctx->y_ready, s));
                 ORB_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->y_ready, 0));
                 ORB_CUDA(cudaMemcpyAsync(ctx->yraw.p, y, n * sizeof(float), cudaMemcpyHostToDevice,
