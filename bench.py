@@ -66,8 +66,8 @@ def workload_name(kind: str, n: int, d: int) -> str:
     return f"plain ORB, {lg(n)} {what}, {lg(d)} leaf cells"
 
 
+def workload_config(n: int, d: int, world: int) -> dict:
     """The `config` both arms print (the same keys and values in both, so the lines compare)."""
-    """The `config` both arms print (the driver compares them)."""
     return {"workload": workload_name("uniform", n, d), "particles": n, "leaves": d,
             "levels": d.bit_length() - 1, "parallelism": f"replicas x{world}",
             "l2": "inputs 1.5 GB > 129 MB L2 (no flush needed)" if 12 * n > (129 << 20)
